@@ -1,0 +1,431 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 segmented sort on its headline workload.
+
+Workload (one "step"): the equal-segment sweep -- for every segment length
+2^1 .. 2^20, one instance of n = 2^24 uint32 keys uniform in [0, 2^32) with
+uint32 values = input index, split into n / len equal segments, sorted in
+place through the library's C ABI (segsort_pairs_u32).  Every step sorts
+fresh copies (inputs created before the timed region, each instance 128 MiB,
+so consecutive calls never find their input in the 126 MB L2).
+
+Printed JSON line (rank 0):
+  value       Gkeys/s over the K timed steps, inputs resident in HBM
+  e2e         the same through the Python API with pinned host buffers:
+              host->device copy of keys+values, sort, device->host copy
+  roofline    the dominant kernel phase, algorithmic bytes (read and write
+              every key and value once, plus the offsets) / its CUDA-event
+              time measured live on the launching stream, against the
+              measured HBM copy bandwidth
+  cpu_baseline  the oracle's per-segment std::stable_sort (the reference's
+              CPU algorithm, src/mseq.cu:44-49) on all host threads, on a
+              2^22-key sample of every instance
+  per_len     per segment length: ms, Gkeys/s and fraction of the HBM roofline
+
+--impl reference times that CPU algorithm as the reference arm (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__ as entry  # noqa: E402
+
+METRIC = "segsort Gkeys/s vs segment size, % HBM roofline; batched/served p50/p99 ms"
+WORKLOAD = ("equal-segment sweep: 2^24 uint32 key/value pairs per instance, keys uniform "
+            "in [0,2^32), values = index, segment length 2^1..2^20 (one instance each)")
+BYTES_PER_PAIR = 16  # read key+value once, write key+value once
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--log-n", type=int, default=24)
+    p.add_argument("--lengths", type=str, default="1-20",
+                   help="log2 segment lengths, e.g. 1-20 or 4,8,12")
+    p.add_argument("--cpu-sample-log", type=int, default=22)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def log_lengths(spec: str) -> list[int]:
+    out = []
+    for part in spec.split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            out.extend(range(int(a), int(b) + 1))
+        else:
+            out.append(int(part))
+    return out
+
+
+def peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_launch() -> dict | None:
+    """DRAM bytes per launch of the profiled kernels, from the committed ncu
+    summary (profiles/traffic.json); None until one is committed."""
+    p = ROOT / "profiles" / "traffic.json"
+    try:
+        return json.loads(p.read_text())
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while running."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                   "-lms", "50"]
+            if self.gpu_id:
+                cmd += ["-i", self.gpu_id]
+            self.proc = subprocess.Popen(cmd, stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 8:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sort_sample(O, inst, n_sample: int, lengths: list[int], threads: int) -> tuple[float, int]:
+    """Seconds to sort, with the oracle's std::stable_sort per segment on
+    `threads` threads, the first n_sample pairs of every instance."""
+    total = 0.0
+    keys_done = 0
+    for lg in lengths:
+        ln = 1 << lg
+        m = max(n_sample // ln, 1) * ln
+        keys = inst.uniform_keys(m, seed=1000 + lg, bits=32)
+        off = inst.equal_offsets(m, ln)
+        vals = np.arange(m, dtype=np.uint32)
+        k = keys.copy()
+        v = vals.copy()
+        kp = k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        vp = v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        op = off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        t0 = time.perf_counter()
+        O.lib().oracle_segsort_pairs_u32(kp, vp, m, op, len(off) - 1, threads)
+        total += time.perf_counter() - t0
+        keys_done += m
+    return total, keys_done
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    entry.load_package()
+    inst = importlib.import_module(f"{entry.PKG_NAME}.instances")
+    lengths = log_lengths(args.lengths)
+    threads = O.default_threads()
+    n_sample = 1 << min(args.cpu_sample_log, args.log_n)
+    for _ in range(args.warmup):
+        cpu_sort_sample(O, inst, n_sample, lengths, threads)
+    secs, keys = 0.0, 0
+    for _ in range(args.steps):
+        s, k = cpu_sort_sample(O, inst, n_sample, lengths, threads)
+        secs += s
+        keys += k
+    value = keys / secs / 1e9
+    sample = (f"first {n_sample} pairs (whole segments) of each of the {len(lengths)} "
+              f"instances per step")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gkeys/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": 1 << args.log_n,
+                   "log2_lengths": lengths, "l2": "inputs larger than L2 (CPU arm)"},
+        "cpu_baseline": {"value": value, "unit": "Gkeys/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    pkg = entry.load_package()
+    pkg.build()
+    inst = importlib.import_module(f"{entry.PKG_NAME}.instances")
+    L = pkg.lib()
+    lengths = log_lengths(args.lengths)
+    n = 1 << args.log_n
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- inputs: one fresh copy per (step, length), all resident ----------
+    offsets = {lg: torch.from_numpy(inst.equal_offsets(n, 1 << lg)).to(dev) for lg in lengths}
+    pristine = {lg: inst.device_uniform_keys(n, seed=1000 + lg, bits=32, device=dev)
+                for lg in lengths}
+    ar = torch.arange(n, dtype=torch.int32, device=dev)
+    total_steps = args.warmup + args.steps
+    bufs = [{lg: (pristine[lg].clone(), ar.clone()) for lg in lengths} for _ in range(total_steps)]
+    torch.cuda.synchronize()
+
+    def sort_call(k, v, lg):
+        o = offsets[lg]
+        rc = L.segsort_pairs_u32(k.data_ptr(), v.data_ptr(), n, o.data_ptr(), o.numel() - 1, st)
+        if rc != 0:
+            raise pkg.SegsortError(rc, "segsort_pairs_u32")
+
+    for s in range(args.warmup):
+        for lg in lengths:
+            sort_call(*bufs[s][lg], lg)
+    barrier()
+    if pkg.device_status() != 0:
+        raise RuntimeError("device status reports a bounded wait that gave up")
+
+    # ---- timed region: exactly K steps -------------------------------------
+    evs = {lg: [] for lg in lengths}
+    gpu_uuid = None
+    try:
+        gpu_uuid = str(torch.cuda.get_device_properties(dev).uuid)
+        gpu_uuid = gpu_uuid if gpu_uuid.startswith("GPU-") else "GPU-" + gpu_uuid
+    except Exception:
+        gpu_uuid = None
+    with ClockSampler(gpu_uuid) as clocks:
+        barrier()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for s in range(args.warmup, total_steps):
+            for lg in lengths:
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                sort_call(*bufs[s][lg], lg)
+                b.record(stream)
+                evs[lg].append((a, b))
+        t_end.record(stream)
+        barrier()
+    region_ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        t = torch.tensor([region_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        region_ms = float(t.item())
+    keys_per_step = n * len(lengths)
+    value = keys_per_step * args.steps * world / (region_ms * 1e-3) / 1e9
+    if pkg.device_status() != 0:
+        raise RuntimeError("device status reports a bounded wait that gave up")
+
+    peak, peak_kind = peak_hbm()
+    per_len = []
+    for lg in lengths:
+        ms = statistics.median(a.elapsed_time(b) for a, b in evs[lg])
+        gbs = (BYTES_PER_PAIR * n + 4 * (n // (1 << lg) + 1)) / (ms * 1e-3) / 1e9
+        per_len.append({"log2_len": lg, "ms": round(ms, 5),
+                        "gkeys_s": round(n / (ms * 1e-3) / 1e9, 3),
+                        "hbm_frac": round(gbs / peak, 4)})
+    del bufs
+
+    # ---- phase profile (one more step on fresh copies) ---------------------
+    pkg.profile_enable(True)
+    pkg.profile_read(reset=True)
+    phase = {}
+    for lg in lengths:
+        k, v = pristine[lg].clone(), ar.clone()
+        torch.cuda.synchronize()
+        sort_call(k, v, lg)
+        torch.cuda.synchronize()
+        phase[lg] = pkg.profile_read(reset=True)
+    pkg.profile_enable(False)
+    cap = 4096  # tile capacity of 32-bit keys: longer segments take the large path
+    tile_ms = sum(p["tile_ms"] for p in phase.values())
+    large_ms = sum(p["large_ms"] for p in phase.values())
+    launches_per_step = sum(p["tile_launches"] + p["large_launches"] for p in phase.values())
+    if tile_ms >= large_ms:
+        name = "tile_sort_kernel"
+        lens_in = [lg for lg in lengths if (1 << lg) <= cap]
+        ms_sum = sum(phase[lg]["tile_ms"] for lg in lens_in)
+        launches = len(lens_in)
+    else:
+        name = "large-segment radix passes (hist + 4 scatter passes)"
+        lens_in = [lg for lg in lengths if (1 << lg) > cap]
+        ms_sum = sum(phase[lg]["large_ms"] for lg in lens_in)
+        launches = len(lens_in)
+    alg_bytes = sum(BYTES_PER_PAIR * n + 4 * (n // (1 << lg) + 1) for lg in lens_in)
+    achieved = alg_bytes / (ms_sum * 1e-3) / 1e9 if ms_sum > 0 else 0.0
+    tr = traffic_per_launch()
+    roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_kind": f"{peak_kind} hbm_gbs (copy)",
+                "algorithmic_bytes_per_launch": alg_bytes // max(launches, 1),
+                "traffic": (tr or {}).get(name.split()[0]) if tr else None,
+                "phase_ms_per_step": {"tile": round(tile_ms, 4), "large": round(large_ms, 4)}}
+
+    # ---- end to end through the public API with host buffers ---------------
+    e2e = None
+    if not args.no_e2e:
+        host = {}
+        for lg in lengths:
+            hk = torch.empty(n, dtype=torch.int32, pin_memory=True)
+            hk.copy_(pristine[lg].cpu())
+            hv = torch.arange(n, dtype=torch.int32).pin_memory()
+            host[lg] = (hk, hv, torch.empty(n, dtype=torch.int32, pin_memory=True),
+                        torch.empty(n, dtype=torch.int32, pin_memory=True))
+        dk = torch.empty(n, dtype=torch.int32, device=dev)
+        dv = torch.empty(n, dtype=torch.int32, device=dev)
+
+        def e2e_step():
+            for lg in lengths:
+                hk, hv, ok, ov = host[lg]
+                dk.copy_(hk, non_blocking=True)
+                dv.copy_(hv, non_blocking=True)
+                pkg.segsort(dk, offsets[lg], dv, key_type="u32")
+                ok.copy_(dk, non_blocking=True)
+                ov.copy_(dv, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        e_steps = max(1, min(args.steps, 5))
+        barrier()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(e_steps):
+            e2e_step()
+        b.record(stream)
+        barrier()
+        e_ms = a.elapsed_time(b)
+        if world > 1:
+            t = torch.tensor([e_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        e2e = {"value": keys_per_step * e_steps * world / (e_ms * 1e-3) / 1e9, "unit": "Gkeys/s",
+               "h2d_bytes_per_step": 8 * n * len(lengths),
+               "d2h_bytes_per_step": 8 * n * len(lengths),
+               "steps": e_steps, "ms_per_step": e_ms / e_steps}
+        # the host copies read back hold sorted segments with their values
+        lg = lengths[-1]
+        hk, hv, ok, ov = host[lg]
+        seg = min(1 << lg, n)
+        got_k = ok[:seg].numpy().view(np.uint32)
+        got_v = ov[:seg].numpy().view(np.uint32)
+        src_k = hk[:seg].numpy().view(np.uint32)
+        if not (np.all(got_k[:-1] <= got_k[1:]) and np.array_equal(src_k[got_v], got_k)):
+            raise RuntimeError("end-to-end read-back is not the sorted segment")
+
+    # ---- CPU baseline (rank 0) ----------------------------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        O.build()
+        threads = O.default_threads()
+        n_sample = 1 << min(args.cpu_sample_log, args.log_n)
+        secs, keys = cpu_sort_sample(O, inst, n_sample, lengths, threads)
+        cpu = {"value": keys / secs / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
+               "sample": f"first {n_sample} pairs (whole segments) of each instance, "
+                         f"{len(lengths)} instances, std::stable_sort per segment on "
+                         f"{threads} threads"}
+
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": region_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "log2_lengths": lengths,
+                       "l2": "inputs larger than L2: 128 MiB fresh instance per call",
+                       "parallelism": f"replicas{world}"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks.summary(), "per_len": per_len,
+        }), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

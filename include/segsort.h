@@ -1,0 +1,162 @@
+/*
+ * segsort.h -- C ABI of the GB300 (sm_103a) segmented sort.
+ *
+ * Every entry point sorts, independently and stably, each segment
+ * [offsets[i], offsets[i+1]) of a device array of keys (and, for the
+ * `pairs` forms, the uint32 values that travel with them).  The sort is in
+ * place: on return the input buffers hold the result, as with
+ * bb_segsort (src/bb_segsort/bb_segsort.h:175-178 copies the result back
+ * into keys_d/vals_d).  Elements outside every segment are not touched.
+ *
+ * Order.  Keys are compared through an order-preserving map to unsigned
+ * bits: unsigned keys as-is, signed keys with the sign bit flipped, float
+ * keys with all bits flipped when the sign bit is set and only the sign
+ * bit flipped otherwise.  So -0.0f sorts before +0.0f, and NaNs sort by
+ * their bit pattern (negative NaNs first, positive NaNs last).  Equal keys
+ * keep their input order (stable), which is what the reference's oracle
+ * std::stable_sort gives (src/mseq.cu:44-49, src/bb_segsort/main.cu:152-173).
+ *
+ * Offsets.  `d_offsets` is a device array of nseg+1 int32 CSR offsets:
+ * segment i is [d_offsets[i], d_offsets[i+1]).  They must be
+ * non-decreasing and lie in [0, n]; the kernels clamp every offset into
+ * [0, n] and treat a segment whose end is below its begin as empty, so a
+ * malformed array cannot make them touch memory outside [0, n).  The
+ * `_heads` forms take nseg segment heads instead, the last segment ending
+ * at n (the bb_segsort and moderngpu convention,
+ * src/bb_segsort/bb_segsort.h:35-36, lib/moderngpu/kernel_segsort.hxx:405-415).
+ *
+ * Asynchrony.  Every call is asynchronous on `stream` and makes no host
+ * synchronisation.  Temporary storage comes either from the caller (the
+ * `_ws` forms, sized by segsort_workspace_bytes) or from a library-owned
+ * stream-ordered memory pool (cudaMallocFromPoolAsync / cudaFreeAsync on
+ * `stream`).  Calls on different streams may run concurrently.
+ *
+ * Errors.  0 on success, a negative SEGSORT_ERR_* code otherwise.  No
+ * call throws or exits.  A device-side failure (a bounded wait in a
+ * kernel that gave up) cannot be returned by an asynchronous call; it is
+ * recorded on the device and read back by segsort_device_status().
+ *
+ * Limits.  n < 2^30 elements per call; offsets are int32.
+ */
+#ifndef SEGSORT_H_
+#define SEGSORT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; a null pointer is the legacy default stream. */
+struct CUstream_st;
+typedef struct CUstream_st *segsort_stream_t;
+
+#define SEGSORT_OK 0
+#define SEGSORT_ERR_INVALID_ARG (-1) /* null pointer, n < 0, nseg < 0, ...   */
+#define SEGSORT_ERR_CUDA (-2)        /* a CUDA runtime call or launch failed */
+#define SEGSORT_ERR_TIMEOUT (-3)     /* a bounded device wait gave up        */
+#define SEGSORT_ERR_NO_MEMORY (-4)   /* the workspace could not be allocated */
+#define SEGSORT_ERR_TOO_LARGE (-5)   /* n or a segment exceeds the limits    */
+#define SEGSORT_ERR_WORKSPACE (-6)   /* caller workspace too small/unaligned */
+
+/* ------------------------------------------------------------------------
+ * Keys only.
+ * Replaces the keys-only CPU path `segmented_sorting(uint* vec, uint* seg,
+ * int number_of_segments)` (src/mseq.cu:44-49), which runs std::stable_sort
+ * on every [seg[i], seg[i+1]).
+ * ---------------------------------------------------------------------- */
+int segsort_keys_u32(uint32_t *d_keys, int64_t n, const int32_t *d_offsets,
+                     int32_t nseg, segsort_stream_t stream);
+int segsort_keys_i32(int32_t *d_keys, int64_t n, const int32_t *d_offsets,
+                     int32_t nseg, segsort_stream_t stream);
+int segsort_keys_f32(float *d_keys, int64_t n, const int32_t *d_offsets,
+                     int32_t nseg, segsort_stream_t stream);
+int segsort_keys_u64(uint64_t *d_keys, int64_t n, const int32_t *d_offsets,
+                     int32_t nseg, segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Key/value pairs (uint32 values, moved with their keys).
+ * Replaces cub::DeviceSegmentedRadixSort::SortPairs(d_temp, temp_bytes,
+ * keys_in, keys_out, vals_in, vals_out, n, nseg, d_seg, d_seg + 1) as called
+ * in src/radixseg.cu:121-124 (signature at
+ * lib/cub/device/device_segmented_radix_sort.cuh:140-155): the same CSR
+ * offsets (begin = d_offsets, end = d_offsets + 1), in place instead of
+ * double-buffered, stable, and without the two-phase temp-storage query.
+ * ---------------------------------------------------------------------- */
+int segsort_pairs_u32(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                      const int32_t *d_offsets, int32_t nseg,
+                      segsort_stream_t stream);
+int segsort_pairs_i32(int32_t *d_keys, uint32_t *d_vals, int64_t n,
+                      const int32_t *d_offsets, int32_t nseg,
+                      segsort_stream_t stream);
+int segsort_pairs_f32(float *d_keys, uint32_t *d_vals, int64_t n,
+                      const int32_t *d_offsets, int32_t nseg,
+                      segsort_stream_t stream);
+int segsort_pairs_u64(uint64_t *d_keys, uint32_t *d_vals, int64_t n,
+                      const int32_t *d_offsets, int32_t nseg,
+                      segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Heads-only offsets: d_heads[nseg], segment i = [d_heads[i], d_heads[i+1])
+ * and the last segment ends at n.
+ * Replaces `int bb_segsort(K *keys_d, T *vals_d, int n, int *d_segs,
+ * int length)` (src/bb_segsort/bb_segsort.h:35-36) and
+ * `mgpu::segmented_sort(keys, vals, count, segments, num_segments, comp,
+ * context)` (lib/moderngpu/kernel_segsort.hxx:405-415; driven from
+ * src/mergeseg.cu:79-90,118-119 with heads only).  Unlike bb_segsort the
+ * result is stable and the call returns 0 on success (bb_segsort returns 1).
+ * ---------------------------------------------------------------------- */
+int segsort_pairs_u32_heads(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                            const int32_t *d_heads, int32_t nseg,
+                            segsort_stream_t stream);
+int segsort_keys_u32_heads(uint32_t *d_keys, int64_t n, const int32_t *d_heads,
+                           int32_t nseg, segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Caller-provided workspace.  segsort_workspace_bytes() is an upper bound
+ * for any offsets array with these n / nseg / key and value widths
+ * (key_bytes 4 or 8, val_bytes 0 or 4).  The workspace must be 256-byte
+ * aligned device memory of at least that size; it is used asynchronously
+ * on `stream` and may be reused once the call's work on `stream` is done.
+ * These replace the two-phase `d_temp_storage == NULL` size query of
+ * lib/cub/device/device_segmented_radix_sort.cuh:140-155.
+ * ---------------------------------------------------------------------- */
+size_t segsort_workspace_bytes(int64_t n, int32_t nseg, int key_bytes,
+                               int val_bytes);
+int segsort_pairs_u32_ws(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                         const int32_t *d_offsets, int32_t nseg,
+                         void *d_workspace, size_t workspace_bytes,
+                         segsort_stream_t stream);
+int segsort_keys_u32_ws(uint32_t *d_keys, int64_t n, const int32_t *d_offsets,
+                        int32_t nseg, void *d_workspace,
+                        size_t workspace_bytes, segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Diagnostics.
+ * segsort_device_status() synchronises the current device, returns
+ * SEGSORT_OK or the first device-side error recorded since the last clear
+ * (SEGSORT_ERR_TIMEOUT when a bounded wait gave up), and clears it when
+ * `clear` is non-zero.  There is no counterpart in the reference, whose
+ * drivers only print cudaGetLastError (src/radixseg.cu:127-132).
+ * ---------------------------------------------------------------------- */
+int segsort_device_status(int clear);
+const char *segsort_error_string(int code);
+int segsort_version(void);
+
+/* Phase timing for benchmarks.  While enabled, every sort call records CUDA
+ * events on its own stream around its tile-sort kernel and around its
+ * large-segment kernels (a few microseconds of host work per call, no
+ * device synchronisation).  segsort_profile_read() waits for the recorded
+ * events, adds up their elapsed times and launch counts since the last
+ * reset, and resets them when `reset` is non-zero.  No counterpart in the
+ * reference, which times whole driver calls only (src/radixseg.cu:121-137). */
+int segsort_profile_enable(int on);
+int segsort_profile_read(double *tile_ms, double *large_ms, int64_t *tile_launches,
+                         int64_t *large_launches, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEGSORT_H_ */

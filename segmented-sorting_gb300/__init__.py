@@ -1,0 +1,180 @@
+"""GB300 segmented sort -- Python host side.
+
+A thin ctypes layer over the C ABI in include/segsort.h (libsegsort.so,
+built in-tree by build.py).  It mirrors the reference's call shape for the
+path -- sort every segment of a device key array (and the values that move
+with the keys) given a segment-offset array, in place -- as
+cub::DeviceSegmentedRadixSort::SortPairs(keys, vals, n, nseg, d_seg, d_seg+1)
+(src/radixseg.cu:121-124) and bb_segsort(keys_d, vals_d, n, d_segs, nseg)
+(src/bb_segsort/bb_segsort.h:35-36) do.
+
+Device memory and streams come from PyTorch (plumbing only): the functions
+take CUDA tensors and pass their raw device pointers and the current CUDA
+stream to the C ABI.  There is no CPU path: if libsegsort.so is missing the
+import of `lib()` raises, and every call goes to the GPU kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libsegsort.so"
+
+SEGSORT_OK = 0
+SEGSORT_ERR_INVALID_ARG = -1
+SEGSORT_ERR_CUDA = -2
+SEGSORT_ERR_TIMEOUT = -3
+SEGSORT_ERR_NO_MEMORY = -4
+SEGSORT_ERR_TOO_LARGE = -5
+SEGSORT_ERR_WORKSPACE = -6
+
+KEY_TYPES = ("u32", "i32", "f32", "u64")
+
+# Every symbol include/segsort.h declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+SIGNATURES = {
+    **{f"segsort_keys_{t}": ([_P, _I64, _P, _I32, _P], ctypes.c_int) for t in KEY_TYPES},
+    **{f"segsort_pairs_{t}": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int) for t in KEY_TYPES},
+    "segsort_pairs_u32_heads": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int),
+    "segsort_keys_u32_heads": ([_P, _I64, _P, _I32, _P], ctypes.c_int),
+    "segsort_workspace_bytes": ([_I64, _I32, ctypes.c_int, ctypes.c_int], ctypes.c_size_t),
+    "segsort_pairs_u32_ws": ([_P, _P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "segsort_keys_u32_ws": ([_P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "segsort_device_status": ([ctypes.c_int], ctypes.c_int),
+    "segsort_error_string": ([ctypes.c_int], ctypes.c_char_p),
+    "segsort_version": ([], ctypes.c_int),
+    "segsort_profile_enable": ([ctypes.c_int], ctypes.c_int),
+    "segsort_profile_read": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                              ctypes.c_int], ctypes.c_int),
+}
+
+
+class SegsortError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        msg = lib().segsort_error_string(code).decode() if LIB_PATH.exists() else str(code)
+        super().__init__(f"{what}: {msg} ({code})" if what else f"{msg} ({code})")
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library.  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run build.py (or __graft_entry__.build())")
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def build(verbose: bool = False) -> None:
+    from importlib import util
+    spec = util.spec_from_file_location("_segsort_build", PKG / "build.py")
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build(verbose=verbose)
+
+
+# ---------------------------------------------------------------------------
+# Torch-tensor convenience layer.
+# ---------------------------------------------------------------------------
+def _key_suffix(t) -> str:
+    import torch
+    m = {torch.int32: "i32", torch.float32: "f32", torch.int64: "u64"}
+    if t.dtype in m:
+        return m[t.dtype]
+    if hasattr(torch, "uint32") and t.dtype == torch.uint32:
+        return "u32"
+    if hasattr(torch, "uint64") and t.dtype == torch.uint64:
+        return "u64"
+    raise TypeError(f"unsupported key dtype {t.dtype}")
+
+
+def _stream_ptr(stream) -> int:
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != SEGSORT_OK:
+        raise SegsortError(rc, what)
+
+
+def segsort(keys, offsets, values=None, *, key_type: str | None = None, heads: bool = False,
+            stream=None) -> None:
+    """Sort every segment of `keys` (and `values`) in place on the GPU.
+
+    keys     CUDA tensor, contiguous; its dtype picks the key type unless
+             `key_type` ("u32", "i32", "f32", "u64") reinterprets its bits
+             (e.g. an int32 tensor holding uint32 keys with key_type="u32").
+    offsets  CUDA int32 tensor: nseg+1 CSR offsets, or nseg heads with heads=True.
+    values   optional CUDA tensor of 32-bit values (uint32 bits) moved with keys.
+    """
+    if not keys.is_cuda or not offsets.is_cuda:
+        raise ValueError("keys and offsets must be CUDA tensors")
+    if not keys.is_contiguous() or not offsets.is_contiguous():
+        raise ValueError("keys and offsets must be contiguous")
+    import torch
+    if offsets.dtype != torch.int32:
+        raise TypeError("offsets must be int32")
+    suf = key_type or _key_suffix(keys)
+    n = keys.numel()
+    nseg = offsets.numel() - (0 if heads else 1)
+    if nseg < 0:
+        raise ValueError("offsets must hold nseg+1 entries")
+    L = lib()
+    st = _stream_ptr(stream)
+    if values is None:
+        if heads:
+            if suf != "u32":
+                raise ValueError("heads-only offsets support u32 keys")
+            rc = L.segsort_keys_u32_heads(keys.data_ptr(), n, offsets.data_ptr(), nseg, st)
+        else:
+            rc = getattr(L, f"segsort_keys_{suf}")(keys.data_ptr(), n, offsets.data_ptr(), nseg, st)
+    else:
+        if values.numel() != n or not values.is_cuda or values.element_size() != 4:
+            raise ValueError("values must be a CUDA tensor of n 32-bit elements")
+        if heads:
+            if suf != "u32":
+                raise ValueError("heads-only offsets support u32 keys")
+            rc = L.segsort_pairs_u32_heads(keys.data_ptr(), values.data_ptr(), n,
+                                           offsets.data_ptr(), nseg, st)
+        else:
+            rc = getattr(L, f"segsort_pairs_{suf}")(keys.data_ptr(), values.data_ptr(), n,
+                                                     offsets.data_ptr(), nseg, st)
+    _check(rc, f"segsort_{'pairs' if values is not None else 'keys'}_{suf}")
+
+
+def device_status(clear: bool = True) -> int:
+    """Synchronise and return the device-side status (0 = no bounded wait gave up)."""
+    return lib().segsort_device_status(1 if clear else 0)
+
+
+def workspace_bytes(n: int, nseg: int, key_bytes: int = 4, val_bytes: int = 4) -> int:
+    return lib().segsort_workspace_bytes(n, nseg, key_bytes, val_bytes)
+
+
+def profile_enable(on: bool = True) -> None:
+    lib().segsort_profile_enable(1 if on else 0)
+
+
+def profile_read(reset: bool = True) -> dict:
+    """Phase times (ms) and kernel launch counts accumulated while enabled."""
+    t, l = ctypes.c_double(), ctypes.c_double()
+    nt, nl = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().segsort_profile_read(ctypes.byref(t), ctypes.byref(l), ctypes.byref(nt),
+                                      ctypes.byref(nl), 1 if reset else 0), "profile_read")
+    return {"tile_ms": t.value, "large_ms": l.value, "tile_launches": nt.value,
+            "large_launches": nl.value}

@@ -1,0 +1,396 @@
+// C ABI of the segmented sort: argument checks, workspace layout, the
+// stream-ordered workspace pool and the launch sequence.  One translation
+// unit holds every kernel so that the device status word is a single symbol.
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "segsort.h"
+#include "segsort_common.cuh"
+#include "tile_sort.cuh"
+#include "large_sort.cuh"
+
+namespace segsort {
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+// ---------------------------------------------------------------------------
+// Tile-sort shape per key width: 4096-element chunks for 32-bit keys (256
+// threads x 16 words), 2048 for 64-bit keys (256 threads x 8 words).
+template <typename K, bool PAIRS>
+struct TileFor {
+  using Cfg = TileConfig<K, PAIRS, 256, sizeof(K) == 4 ? 16 : 8>;
+};
+
+template <typename K>
+constexpr int64_t tile_cap() {
+  return TileFor<K, false>::Cfg::CAP;
+}
+
+// ---------------------------------------------------------------------------
+// Workspace layout (every region 256-byte aligned).
+struct WsLayout {
+  size_t ctr = 0, list = 0, prefix = 0, hist = 0, status = 0, tmp_keys = 0, tmp_vals = 0;
+  size_t total = 0;
+  int32_t max_large = 0;
+  int64_t max_chunks = 0;
+  int passes = 0;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t cap, int64_t chunk) {
+  WsLayout L;
+  if (n <= cap) return L;  // no segment can exceed the tile capacity
+  L.max_large = static_cast<int32_t>(n / (cap + 1) + 1);
+  L.max_chunks = n / chunk + L.max_large + 1;
+  L.passes = key_bytes;  // 8-bit digits
+  size_t off = 0;
+  L.ctr = off;      off = align256(off + kCtrWords * sizeof(uint32_t));
+  L.list = off;     off = align256(off + static_cast<size_t>(L.max_large) * 4);
+  L.prefix = off;   off = align256(off + static_cast<size_t>(L.max_large + 1) * 4);
+  L.hist = off;     off = align256(off + static_cast<size_t>(L.max_large) * L.passes * kRadix * 4);
+  L.status = off;   off = align256(off + static_cast<size_t>(L.max_chunks) * L.passes * kRadix * 4);
+  L.tmp_keys = off; off = align256(off + static_cast<size_t>(n) * key_bytes);
+  L.tmp_vals = off; off = align256(off + static_cast<size_t>(n) * val_bytes);
+  L.total = off;
+  return L;
+}
+
+template <typename K, bool PAIRS>
+WsLayout layout_for(int64_t n) {
+  return make_layout(n, sizeof(K), PAIRS ? 4 : 0, tile_cap<K>(), PassShape<K>::kChunk);
+}
+
+// ---------------------------------------------------------------------------
+// Per-device state: SM count and a library-owned memory pool that keeps its
+// memory between calls (release threshold = max), so stream-ordered
+// allocations after the first are cheap and never synchronise.
+struct DeviceState {
+  std::once_flag once;
+  int sms = 0;
+  cudaMemPool_t pool = nullptr;
+  cudaError_t init_err = cudaSuccess;
+};
+DeviceState g_dev[kMaxDevices];
+
+DeviceState *device_state(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) return nullptr;
+  DeviceState &S = g_dev[dev];
+  std::call_once(S.once, [&] {
+    cudaError_t e = cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { S.init_err = e; return; }
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    e = cudaMemPoolCreate(&S.pool, &props);
+    if (e != cudaSuccess) { S.init_err = e; return; }
+    uint64_t thr = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(S.pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (e != cudaSuccess) S.init_err = e;
+  });
+  return S.init_err == cudaSuccess ? &S : nullptr;
+}
+
+// Opt a kernel into more than 48 KB of dynamic shared memory once per device.
+template <typename Kern>
+cudaError_t ensure_smem(Kern kernel, size_t bytes, std::atomic<uint64_t> &done, int dev) {
+  const uint64_t bit = 1ull << dev;
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(bytes));
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+  return e;
+}
+
+// Resident CTAs per SM of a kernel, cached per device.
+template <typename Kern>
+int occupancy(Kern kernel, int threads, size_t smem, std::atomic<int> (&cache)[kMaxDevices],
+              int dev) {
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, smem) != cudaSuccess ||
+      v < 1)
+    v = 1;
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Opt-in phase timing (segsort_profile_enable / segsort_profile_read).
+struct PhaseRecord {
+  cudaEvent_t t0 = nullptr, t1 = nullptr, l0 = nullptr, l1 = nullptr;
+  int large_launches = 0;
+};
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
+std::vector<PhaseRecord> g_prof_pending;
+double g_prof_tile_ms = 0.0, g_prof_large_ms = 0.0;
+int64_t g_prof_tile_launches = 0, g_prof_large_launches = 0;
+
+cudaEvent_t prof_event(cudaStream_t stream) {
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  if (cudaEventRecord(e, stream) != cudaSuccess) {
+    cudaEventDestroy(e);
+    return nullptr;
+  }
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+template <typename K, bool PAIRS>
+int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_t nseg,
+              bool heads, void *ws, size_t ws_bytes, cudaStream_t stream) {
+  if (n < 0 || nseg < 0) return SEGSORT_ERR_INVALID_ARG;
+  if (n == 0 || nseg == 0) return SEGSORT_OK;
+  if (keys == nullptr || offsets == nullptr || (PAIRS && vals == nullptr))
+    return SEGSORT_ERR_INVALID_ARG;
+  if (n >= (int64_t{1} << 30)) return SEGSORT_ERR_TOO_LARGE;
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  DeviceState *S = device_state(dev);
+  if (S == nullptr) return SEGSORT_ERR_CUDA;
+
+  const Offsets off{offsets, nseg, heads ? 1 : 0, n};
+
+  // ---- tile sort: every segment of at most CAP elements -------------------
+  using Cfg = typename TileFor<K, PAIRS>::Cfg;
+  auto tile_kernel = tile_sort_kernel<K, PAIRS, Cfg::NT, Cfg::KPT>;
+  static std::atomic<uint64_t> tile_attr_done{0};
+  if (ensure_smem(tile_kernel, Cfg::kSmemBytes, tile_attr_done, dev) != cudaSuccess)
+    return SEGSORT_ERR_CUDA;
+  const bool prof = g_prof_on.load(std::memory_order_relaxed);
+  PhaseRecord rec;
+  if (prof) rec.t0 = prof_event(stream);
+  const int64_t tiles = (n + Cfg::CAP - 1) / Cfg::CAP;
+  tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off);
+  if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+  if (prof) rec.t1 = prof_event(stream);
+
+  // ---- large segments ------------------------------------------------------
+  const WsLayout L = layout_for<K, PAIRS>(n);
+  if (L.total == 0) {
+    if (prof) {
+      std::lock_guard<std::mutex> lk(g_prof_mu);
+      g_prof_pending.push_back(rec);
+    }
+    return SEGSORT_OK;
+  }
+
+  bool owned = false;
+  unsigned char *base = static_cast<unsigned char *>(ws);
+  if (base == nullptr) {
+    if (cudaMallocFromPoolAsync(reinterpret_cast<void **>(&base), L.total, S->pool, stream) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return SEGSORT_ERR_NO_MEMORY;
+    }
+    owned = true;
+  } else if (ws_bytes < L.total || (reinterpret_cast<uintptr_t>(base) & 255) != 0) {
+    return SEGSORT_ERR_WORKSPACE;
+  }
+
+  LargeWs<K> W;
+  W.ctr = reinterpret_cast<uint32_t *>(base + L.ctr);
+  W.list = reinterpret_cast<int32_t *>(base + L.list);
+  W.chunk_prefix = reinterpret_cast<int32_t *>(base + L.prefix);
+  W.hist = reinterpret_cast<uint32_t *>(base + L.hist);
+  W.status = reinterpret_cast<uint32_t *>(base + L.status);
+  W.tmp_keys = reinterpret_cast<K *>(base + L.tmp_keys);
+  W.tmp_vals = PAIRS ? reinterpret_cast<uint32_t *>(base + L.tmp_vals) : nullptr;
+  W.max_large = L.max_large;
+  W.passes = L.passes;
+  W.max_chunks = L.max_chunks;
+
+  int rc = SEGSORT_OK;
+  if (prof) rec.l0 = prof_event(stream);
+  do {
+    if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess) {
+      rc = SEGSORT_ERR_CUDA;
+      break;
+    }
+    const unsigned cls_blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 255) / 256);
+    large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), W);
+    large_scan_kernel<K><<<1, 1024, 0, stream>>>(W);
+
+    static std::atomic<int> hist_occ[kMaxDevices];
+    static std::atomic<int> pass_occ[kMaxDevices];
+    const int ho = occupancy(large_hist_kernel<K>, kPassThreads, 0, hist_occ, dev);
+    const int po = occupancy(large_pass_kernel<K, PAIRS>, kPassThreads, 0, pass_occ, dev);
+    const int64_t hist_grid = std::min<int64_t>(L.max_chunks, static_cast<int64_t>(ho) * S->sms);
+    const int64_t pass_grid = std::min<int64_t>(L.max_chunks, static_cast<int64_t>(po) * S->sms);
+    large_hist_kernel<K><<<static_cast<unsigned>(hist_grid), kPassThreads, 0, stream>>>(keys, off, W);
+    for (int p = 0; p < L.passes; ++p) {
+      const bool even = (p & 1) == 0;
+      const K *sk = even ? keys : W.tmp_keys;
+      K *dk = even ? W.tmp_keys : keys;
+      const uint32_t *sv = PAIRS ? (even ? vals : W.tmp_vals) : nullptr;
+      uint32_t *dv = PAIRS ? (even ? W.tmp_vals : vals) : nullptr;
+      large_pass_kernel<K, PAIRS><<<static_cast<unsigned>(pass_grid), kPassThreads, 0, stream>>>(
+          sk, sv, dk, dv, off, W, p);
+    }
+    if (cudaGetLastError() != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+  } while (false);
+  if (prof) {
+    rec.l1 = prof_event(stream);
+    rec.large_launches = 3 + L.passes;  // classify, scan, hist, one per pass
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_pending.push_back(rec);
+  }
+
+  if (owned && cudaFreeAsync(base, stream) != cudaSuccess && rc == SEGSORT_OK) rc = SEGSORT_ERR_CUDA;
+  return rc;
+}
+
+template <typename K, bool PAIRS>
+size_t workspace_bytes_for(int64_t n) {
+  return layout_for<K, PAIRS>(n).total;
+}
+
+}  // namespace
+}  // namespace segsort
+
+using segsort::sort_impl;
+
+extern "C" {
+
+#define SEGSORT_ST(s) reinterpret_cast<cudaStream_t>(s)
+
+int segsort_keys_u32(uint32_t *k, int64_t n, const int32_t *o, int32_t ns, segsort_stream_t s) {
+  return sort_impl<uint32_t, false>(k, nullptr, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_keys_i32(int32_t *k, int64_t n, const int32_t *o, int32_t ns, segsort_stream_t s) {
+  return sort_impl<int32_t, false>(k, nullptr, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_keys_f32(float *k, int64_t n, const int32_t *o, int32_t ns, segsort_stream_t s) {
+  return sort_impl<float, false>(k, nullptr, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_keys_u64(uint64_t *k, int64_t n, const int32_t *o, int32_t ns, segsort_stream_t s) {
+  return sort_impl<uint64_t, false>(k, nullptr, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+
+int segsort_pairs_u32(uint32_t *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                      segsort_stream_t s) {
+  return sort_impl<uint32_t, true>(k, v, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_pairs_i32(int32_t *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                      segsort_stream_t s) {
+  return sort_impl<int32_t, true>(k, v, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_pairs_f32(float *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                      segsort_stream_t s) {
+  return sort_impl<float, true>(k, v, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_pairs_u64(uint64_t *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                      segsort_stream_t s) {
+  return sort_impl<uint64_t, true>(k, v, n, o, ns, false, nullptr, 0, SEGSORT_ST(s));
+}
+
+int segsort_pairs_u32_heads(uint32_t *k, uint32_t *v, int64_t n, const int32_t *h, int32_t ns,
+                            segsort_stream_t s) {
+  return sort_impl<uint32_t, true>(k, v, n, h, ns, true, nullptr, 0, SEGSORT_ST(s));
+}
+int segsort_keys_u32_heads(uint32_t *k, int64_t n, const int32_t *h, int32_t ns,
+                           segsort_stream_t s) {
+  return sort_impl<uint32_t, false>(k, nullptr, n, h, ns, true, nullptr, 0, SEGSORT_ST(s));
+}
+
+size_t segsort_workspace_bytes(int64_t n, int32_t nseg, int key_bytes, int val_bytes) {
+  (void)nseg;
+  if (n <= 0) return 0;
+  const bool pairs = val_bytes != 0;
+  if (key_bytes == 8)
+    return pairs ? segsort::workspace_bytes_for<uint64_t, true>(n)
+                 : segsort::workspace_bytes_for<uint64_t, false>(n);
+  return pairs ? segsort::workspace_bytes_for<uint32_t, true>(n)
+               : segsort::workspace_bytes_for<uint32_t, false>(n);
+}
+
+int segsort_pairs_u32_ws(uint32_t *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                         void *ws, size_t ws_bytes, segsort_stream_t s) {
+  if (ws == nullptr && segsort_workspace_bytes(n, ns, 4, 4) != 0) return SEGSORT_ERR_WORKSPACE;
+  return sort_impl<uint32_t, true>(k, v, n, o, ns, false, ws, ws_bytes, SEGSORT_ST(s));
+}
+int segsort_keys_u32_ws(uint32_t *k, int64_t n, const int32_t *o, int32_t ns, void *ws,
+                        size_t ws_bytes, segsort_stream_t s) {
+  if (ws == nullptr && segsort_workspace_bytes(n, ns, 4, 0) != 0) return SEGSORT_ERR_WORKSPACE;
+  return sort_impl<uint32_t, false>(k, nullptr, n, o, ns, false, ws, ws_bytes, SEGSORT_ST(s));
+}
+
+int segsort_device_status(int clear) {
+  if (cudaDeviceSynchronize() != cudaSuccess) return SEGSORT_ERR_CUDA;
+  uint32_t v = 0;
+  if (cudaMemcpyFromSymbol(&v, segsort::g_device_status, sizeof(v)) != cudaSuccess)
+    return SEGSORT_ERR_CUDA;
+  if (clear) {
+    const uint32_t zero = 0;
+    if (cudaMemcpyToSymbol(segsort::g_device_status, &zero, sizeof(zero)) != cudaSuccess)
+      return SEGSORT_ERR_CUDA;
+  }
+  return (v & segsort::kStatusTimeout) ? SEGSORT_ERR_TIMEOUT : SEGSORT_OK;
+}
+
+const char *segsort_error_string(int code) {
+  switch (code) {
+    case SEGSORT_OK: return "ok";
+    case SEGSORT_ERR_INVALID_ARG: return "invalid argument";
+    case SEGSORT_ERR_CUDA: return "CUDA runtime error";
+    case SEGSORT_ERR_TIMEOUT: return "bounded device wait timed out";
+    case SEGSORT_ERR_NO_MEMORY: return "workspace allocation failed";
+    case SEGSORT_ERR_TOO_LARGE: return "problem exceeds the supported size";
+    case SEGSORT_ERR_WORKSPACE: return "caller workspace too small or misaligned";
+    default: return "unknown error";
+  }
+}
+
+int segsort_version(void) { return 100; }
+
+int segsort_profile_enable(int on) {
+  segsort::g_prof_on.store(on != 0, std::memory_order_relaxed);
+  return SEGSORT_OK;
+}
+
+int segsort_profile_read(double *tile_ms, double *large_ms, int64_t *tile_launches,
+                         int64_t *large_launches, int reset) {
+  using namespace segsort;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  int rc = SEGSORT_OK;
+  auto span = [&](cudaEvent_t a, cudaEvent_t b) -> double {
+    float ms = 0.f;
+    if (a && b) {
+      if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+        rc = SEGSORT_ERR_CUDA;
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    return ms;
+  };
+  for (PhaseRecord &r : g_prof_pending) {
+    g_prof_tile_ms += span(r.t0, r.t1);
+    g_prof_tile_launches += 1;
+    if (r.l0 || r.l1) {
+      g_prof_large_ms += span(r.l0, r.l1);
+      g_prof_large_launches += r.large_launches;
+    }
+  }
+  g_prof_pending.clear();
+  if (tile_ms) *tile_ms = g_prof_tile_ms;
+  if (large_ms) *large_ms = g_prof_large_ms;
+  if (tile_launches) *tile_launches = g_prof_tile_launches;
+  if (large_launches) *large_launches = g_prof_large_launches;
+  if (reset) {
+    g_prof_tile_ms = g_prof_large_ms = 0.0;
+    g_prof_tile_launches = g_prof_large_launches = 0;
+  }
+  return rc;
+}
+
+}  // extern "C"

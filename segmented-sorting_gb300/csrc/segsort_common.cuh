@@ -1,0 +1,114 @@
+// Shared device-side pieces of the segmented sort: the order-preserving key
+// maps, the offsets accessor, the device status word and small helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "segsort.h"
+
+namespace segsort {
+
+// ---------------------------------------------------------------------------
+// Order-preserving maps between a key and unsigned "order bits".  Sorting the
+// bits as unsigned integers sorts the keys.  The signed rule is the sign-bit
+// flip of CUB's RadixTraits::TwiddleIn (lib/cub/util_type.cuh:937-949); the
+// float rule flips every bit of negative values and only the sign bit of the
+// others, so -0.0 < +0.0 and NaNs order by bit pattern.
+// ---------------------------------------------------------------------------
+template <typename K> struct KeyOrder;
+
+template <> struct KeyOrder<uint32_t> {
+  using Bits = uint32_t;
+  static __host__ __device__ __forceinline__ Bits to_bits(uint32_t k) { return k; }
+  static __host__ __device__ __forceinline__ uint32_t from_bits(Bits b) { return b; }
+};
+
+template <> struct KeyOrder<int32_t> {
+  using Bits = uint32_t;
+  static __host__ __device__ __forceinline__ Bits to_bits(int32_t k) {
+    return static_cast<uint32_t>(k) ^ 0x80000000u;
+  }
+  static __host__ __device__ __forceinline__ int32_t from_bits(Bits b) {
+    return static_cast<int32_t>(b ^ 0x80000000u);
+  }
+};
+
+template <> struct KeyOrder<float> {
+  using Bits = uint32_t;
+  static __device__ __forceinline__ Bits to_bits(float k) {
+    uint32_t u = __float_as_uint(k);
+    uint32_t mask = (u & 0x80000000u) ? 0xFFFFFFFFu : 0x80000000u;
+    return u ^ mask;
+  }
+  static __device__ __forceinline__ float from_bits(Bits b) {
+    uint32_t mask = (b & 0x80000000u) ? 0x80000000u : 0xFFFFFFFFu;
+    return __uint_as_float(b ^ mask);
+  }
+};
+
+template <> struct KeyOrder<uint64_t> {
+  using Bits = uint64_t;
+  static __host__ __device__ __forceinline__ Bits to_bits(uint64_t k) { return k; }
+  static __host__ __device__ __forceinline__ uint64_t from_bits(Bits b) { return b; }
+};
+
+// ---------------------------------------------------------------------------
+// Segment offsets.  off(i) for i in [0, nseg] is the begin of segment i (and
+// the end of segment i-1).  CSR arrays hold nseg+1 entries; heads-only arrays
+// hold nseg and the end of the last segment is n.  Every value is clamped into
+// [0, n], so malformed offsets cannot address memory outside the arrays.
+// ---------------------------------------------------------------------------
+struct Offsets {
+  const int32_t *p;
+  int32_t nseg;
+  int32_t heads;  // 1: heads-only array of nseg entries
+  int64_t n;
+
+  __device__ __forceinline__ int64_t operator()(int64_t i) const {
+    int64_t v = (heads && i >= nseg) ? n : static_cast<int64_t>(__ldg(p + i));
+    v = v < 0 ? 0 : v;
+    return v > n ? n : v;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Device status word: kernels OR error bits into it; the host reads it back
+// with segsort_device_status().
+// ---------------------------------------------------------------------------
+enum : uint32_t {
+  kStatusTimeout = 1u,
+};
+
+// Defined here: the library is one translation unit (segsort_api.cu), which
+// is the only file that includes this header.
+__device__ uint32_t g_device_status = 0;
+
+__device__ __forceinline__ void raise_status(uint32_t bits) {
+  atomicOr(&g_device_status, bits);
+}
+
+// Largest index j in [lo, hi] with off(j) <= limit (off non-decreasing and
+// off(lo) <= limit).
+__device__ __forceinline__ int64_t last_offset_le(const Offsets &off, int64_t lo,
+                                                  int64_t hi, int64_t limit) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi + 1) >> 1;
+    if (off(mid) <= limit) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// First index s in [0, nseg] with off(s) >= pos (nseg if none).
+__device__ __forceinline__ int64_t first_offset_ge(const Offsets &off, int64_t pos) {
+  int64_t lo = 0, hi = off.nseg;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (off(mid) < pos) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
+
+}  // namespace segsort

@@ -1,0 +1,150 @@
+"""Seeded synthetic instances for the segmented sort (numpy, host side).
+
+Every value is a function of (seed, index) through splitmix64, the same
+counter-based stream csrc/gen_instance.cpp uses, so instances are identical
+on every machine and between the Python and C++ generators (lognormal
+lengths go through floating-point exp/log/cos and may differ by one in rare
+rounding cases; keys and equal/diff offsets are exact integer arithmetic).
+
+Workloads (the reference's sweep shapes, scripts/genequalseg.sh:3-16, and
+the benchmark configurations built on them):
+  equal_offsets      n / len equal segments (utils/gen_equal.cpp:13-16)
+  diff_offsets       nseg random distinct cut points (utils/gen_diff.cpp:11-42)
+  lognormal_offsets  lognormal(mu, sigma) lengths clipped to [1, max], summed
+                     to n, the last one truncated, plus ~empty_frac empty ones
+  uniform_keys       keys uniform in [0, 2^bits)
+  zipf_keys          Zipf(a) ranks via the inverse CDF of the continuous power
+                     law, truncated to uint32 (heavily repeated small keys)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+_LANE = np.uint64(0xD1B54A32D192ED03)
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        x = x.astype(np.uint64) + _GOLD
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+
+def draw(seed: int, lane: int, start: int, count: int) -> np.ndarray:
+    """Values start..start+count-1 of the counter-based stream (seed, lane)."""
+    with np.errstate(over="ignore"):
+        base = np.uint64(seed) * _GOLD + np.uint64(lane) * _LANE + np.uint64(start + 1)
+        return splitmix64(base + np.arange(count, dtype=np.uint64))
+
+
+def _unit(r: np.ndarray) -> np.ndarray:
+    return ((r >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def uniform_keys(n: int, seed: int = 1, bits: int = 32, dtype=np.uint32) -> np.ndarray:
+    """Keys uniform in [0, 2^bits): the top `bits` bits of the stream."""
+    r = draw(seed, 0, 0, n)
+    if bits < 64:
+        r = r >> np.uint64(64 - bits)
+    return r.astype(dtype)
+
+
+def zipf_keys(n: int, seed: int = 1, a: float = 1.1) -> np.ndarray:
+    u = _unit(draw(seed, 5, 0, n))
+    with np.errstate(over="ignore"):
+        r = np.floor(u ** (-1.0 / (a - 1.0)))
+    return np.minimum(r, 4294967295.0).astype(np.uint32)
+
+
+def equal_offsets(n: int, length: int) -> np.ndarray:
+    nseg = n // length
+    return (np.arange(nseg + 1, dtype=np.int64) * length).astype(np.int32)
+
+
+def diff_offsets(n: int, nseg: int, seed: int = 1) -> np.ndarray:
+    """nseg segments cut at nseg-1 distinct random points of [1, n), sorted."""
+    if nseg < 1 or nseg > n:
+        raise ValueError("need 1 <= nseg <= n")
+    taken = np.zeros(n, dtype=bool)
+    taken[0] = True
+    cuts = [0]
+    i = 0
+    while len(cuts) < nseg:
+        need = nseg - len(cuts)
+        r = (draw(seed, 1, i, 2 * need + 16) % np.uint64(n)).astype(np.int64)
+        i += len(r)
+        for x in r:
+            if not taken[x]:
+                taken[x] = True
+                cuts.append(int(x))
+                if len(cuts) == nseg:
+                    break
+    return np.concatenate([np.sort(np.array(cuts, dtype=np.int64)), [n]]).astype(np.int32)
+
+
+def lognormal_offsets(n: int, seed: int = 1, mu: float = 4.0, sigma: float = 2.5,
+                      max_len: int = 1 << 22, empty_frac: float = 0.01) -> np.ndarray:
+    lens = []
+    total = 0
+    i = 0
+    while total < n:
+        m = 4096
+        u = _unit(draw(seed, 2, 2 * i, 2 * m))
+        u1, u2 = u[0::2], u[1::2]
+        z = np.sqrt(-2.0 * np.log(u1)) * np.cos(6.283185307179586 * u2)
+        ln = np.clip(np.rint(np.exp(mu + sigma * z)), 1, max_len).astype(np.int64)
+        for x in ln:
+            x = min(int(x), n - total)
+            lens.append(x)
+            total += x
+            if total >= n:
+                break
+        i += m
+    lens = np.array(lens, dtype=np.int64)
+    ends = np.cumsum(lens)
+    empty = _unit(draw(seed, 3, 0, len(lens))) < empty_frac
+    # segment i is followed by an empty segment when empty[i]
+    reps = np.where(empty, 2, 1)
+    off = np.concatenate([[0], np.repeat(ends, reps)])
+    return off.astype(np.int32)
+
+
+def instance(workload: str, n: int, seed: int = 1, length: int = 0, nseg: int = 0,
+             bits: int = 32):
+    """(offsets, keys) of a named workload."""
+    if workload == "equal":
+        return equal_offsets(n, length), uniform_keys(n, seed, bits)
+    if workload == "diff":
+        return diff_offsets(n, nseg, seed), uniform_keys(n, seed, bits)
+    if workload == "lognormal":
+        return lognormal_offsets(n, seed), uniform_keys(n, seed, bits)
+    if workload == "lognormal-zipf":
+        return lognormal_offsets(n, seed), zipf_keys(n, seed)
+    raise ValueError(workload)
+
+
+# ---------------------------------------------------------------------------
+# Device-side generation (torch int64 arithmetic wraps like uint64; logical
+# shifts are emulated with masks).  Produces exactly uniform_keys(n, seed, bits).
+def _s64(x: int) -> int:
+    x &= (1 << 64) - 1
+    return x - (1 << 64) if x >= (1 << 63) else x
+
+
+def _srl(t, k: int):
+    return (t >> k) & ((1 << (64 - k)) - 1)
+
+
+def device_uniform_keys(n: int, seed: int = 1, bits: int = 32, device="cuda"):
+    """int32 CUDA tensor holding the uint32 bits of uniform_keys(n, seed, bits)."""
+    import torch
+    base = _s64(seed * 0x9E3779B97F4A7C15 + 1)
+    x = torch.arange(n, dtype=torch.int64, device=device) + base
+    x = x + _s64(0x9E3779B97F4A7C15)
+    x = (x ^ _srl(x, 30)) * _s64(0xBF58476D1CE4E5B9)
+    x = (x ^ _srl(x, 27)) * _s64(0x94D049BB133111EB)
+    x = x ^ _srl(x, 31)
+    k = _srl(x, 64 - bits)
+    return (k - (k >= (1 << 31)).to(torch.int64) * (1 << 32)).to(torch.int32)

@@ -1,0 +1,90 @@
+"""CPU: the C-ABI library builds for sm_103a, loads, and exports every entry
+point include/segsort.h declares.  Only host-side paths run here (argument
+checks that return before any CUDA call, sizes, strings); no kernel runs."""
+from __future__ import annotations
+
+import ctypes
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = ROOT / "include" / "segsort.h"
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(segsort_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for must in ("segsort_keys_u32", "segsort_pairs_u32", "segsort_pairs_u32_heads",
+                 "segsort_workspace_bytes", "segsort_device_status"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(pkg.LIB_PATH)],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (segsort_\w+)", out))
+    missing = [f for f in declared_functions() if f not in exported]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_header(pkg):
+    assert set(declared_functions()) == set(pkg.SIGNATURES)
+    L = pkg.lib()
+    for name in pkg.SIGNATURES:
+        assert callable(getattr(L, name))
+
+
+def test_library_is_built_for_sm_103a(pkg):
+    out = subprocess.run(["cuobjdump", "--list-elf", str(pkg.LIB_PATH)],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_host_side_argument_checks(pkg):
+    L = pkg.lib()
+    # n == 0 or nseg == 0: nothing to do, no device access
+    assert L.segsort_keys_u32(None, 0, None, 0, None) == pkg.SEGSORT_OK
+    assert L.segsort_pairs_u32(None, None, 0, None, 5, None) == pkg.SEGSORT_OK
+    # negative sizes and null pointers are rejected before any CUDA call
+    assert L.segsort_keys_u32(None, -1, None, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_keys_u32(None, 10, None, -1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_keys_u32(None, 10, None, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_pairs_f32(ctypes.c_void_p(16), None, 10, ctypes.c_void_p(16), 1,
+                               None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_keys_u64(ctypes.c_void_p(16), 1 << 30, ctypes.c_void_p(16), 1,
+                              None) == pkg.SEGSORT_ERR_TOO_LARGE
+    # the explicit-workspace form refuses a missing workspace when one is needed
+    assert L.segsort_pairs_u32_ws(ctypes.c_void_p(16), ctypes.c_void_p(16), 1 << 20,
+                                  ctypes.c_void_p(16), 1, None, 0,
+                                  None) == pkg.SEGSORT_ERR_WORKSPACE
+
+
+def test_workspace_sizes(pkg):
+    L = pkg.lib()
+    # no segment can exceed the tile capacity: no workspace at all
+    assert L.segsort_workspace_bytes(4096, 1, 4, 4) == 0
+    assert L.segsort_workspace_bytes(2048, 1, 8, 4) == 0
+    n = 1 << 24
+    ws_pairs = L.segsort_workspace_bytes(n, 1, 4, 4)
+    ws_keys = L.segsort_workspace_bytes(n, 1, 4, 0)
+    # the ping-pong copy of the keys (and values) dominates
+    assert ws_pairs >= 8 * n and ws_keys >= 4 * n and ws_pairs - ws_keys >= 4 * n
+    assert ws_pairs < 12 * n
+    assert L.segsort_workspace_bytes(n, 1, 8, 4) >= 12 * n
+
+
+def test_error_strings_and_version(pkg):
+    L = pkg.lib()
+    for code in range(0, -7, -1):
+        assert L.segsort_error_string(code)
+    assert L.segsort_version() >= 100
