@@ -22,9 +22,17 @@ constexpr int kMaxDevices = 64;
 // ---------------------------------------------------------------------------
 // Tile-sort shape per key width: 4096-element chunks for 32-bit keys (256
 // threads x 16 words), 2048 for 64-bit keys (256 threads x 8 words).
+// Build-time tuning knobs (defaults are the measured best on GB300).
+#ifndef SEGSORT_TILE_KPT32
+#define SEGSORT_TILE_KPT32 16
+#endif
+#ifndef SEGSORT_TILE_MINB
+#define SEGSORT_TILE_MINB 2
+#endif
 template <typename K, bool PAIRS>
 struct TileFor {
-  using Cfg = TileConfig<K, PAIRS, 256, sizeof(K) == 4 ? 16 : 8>;
+  using Cfg = TileConfig<K, PAIRS, 256, sizeof(K) == 4 ? SEGSORT_TILE_KPT32 : 8>;
+  static constexpr int kMinBlocks = SEGSORT_TILE_MINB;  // resident CTAs per SM the registers must allow
 };
 
 template <typename K>
@@ -35,10 +43,13 @@ constexpr int64_t tile_cap() {
 // ---------------------------------------------------------------------------
 // Workspace layout (every region 256-byte aligned).
 struct WsLayout {
-  size_t ctr = 0, list = 0, prefix = 0, hist = 0, status = 0, tmp_keys = 0, tmp_vals = 0;
+  size_t ctr = 0, jobs0 = 0, jobs1 = 0, prefix = 0, hist = 0, bstart = 0, digit = 0, status = 0,
+         desc = 0, entries = 0, half_first = 0, tmp_keys = 0, tmp_vals = 0;
   size_t total = 0;
-  int32_t max_large = 0;
+  int32_t max_jobs = 0;
   int64_t max_chunks = 0;
+  int64_t max_entries = 0;
+  int64_t halves = 0;
   int passes = 0;
 };
 
@@ -46,18 +57,35 @@ size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t cap, int64_t chunk) {
   WsLayout L;
-  if (n <= cap) return L;  // no segment can exceed the tile capacity
-  L.max_large = static_cast<int32_t>(n / (cap + 1) + 1);
-  L.max_chunks = n / chunk + L.max_large + 1;
+  if (n <= cap) return L;  // one tile: no workspace
+  // Jobs of every level are longer than cap: at most n / (cap + 1) of them.
+  L.max_jobs = static_cast<int32_t>(n / (cap + 1) + 1);
+  L.max_chunks = n / chunk + L.max_jobs + 1;
+  // Bucket chunks: greedy packing gives at most 4 len / cap + 1 per job,
+  // copies at most len / cap + 1.
+  L.max_entries = 5 * (n / cap) + 2 * static_cast<int64_t>(L.max_jobs) + 16;
+  L.halves = 2 * ((n + cap - 1) / cap);
   L.passes = key_bytes;  // 8-bit digits
   size_t off = 0;
-  L.ctr = off;      off = align256(off + kCtrWords * sizeof(uint32_t));
-  L.list = off;     off = align256(off + static_cast<size_t>(L.max_large) * 4);
-  L.prefix = off;   off = align256(off + static_cast<size_t>(L.max_large + 1) * 4);
-  L.hist = off;     off = align256(off + static_cast<size_t>(L.max_large) * L.passes * kRadix * 4);
-  L.status = off;   off = align256(off + static_cast<size_t>(L.max_chunks) * L.passes * kRadix * 4);
-  L.tmp_keys = off; off = align256(off + static_cast<size_t>(n) * key_bytes);
-  L.tmp_vals = off; off = align256(off + static_cast<size_t>(n) * val_bytes);
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align256(off + bytes);
+    return at;
+  };
+  const size_t mj = static_cast<size_t>(L.max_jobs);
+  L.ctr = take(kCtrWords * sizeof(uint32_t));
+  L.jobs0 = take(mj * sizeof(int4));
+  L.jobs1 = take(mj * sizeof(int4));
+  L.prefix = take((mj + 1) * 4);
+  L.hist = take(mj * L.passes * kRadix * 4);
+  L.bstart = take(mj * (kRadix + 1) * 4);
+  L.digit = take(mj * 4);
+  L.status = take(static_cast<size_t>(L.max_chunks) * kRadix * 4);
+  L.desc = take(static_cast<size_t>(L.max_chunks) * sizeof(int4));
+  L.entries = take(static_cast<size_t>(L.max_entries) * sizeof(int4));
+  L.half_first = take(static_cast<size_t>(L.halves + 1) * 4);
+  L.tmp_keys = take(static_cast<size_t>(n) * key_bytes);
+  L.tmp_vals = take(static_cast<size_t>(n) * val_bytes);
   L.total = off;
   return L;
 }
@@ -74,6 +102,7 @@ WsLayout layout_for(int64_t n) {
 struct DeviceState {
   std::once_flag once;
   int sms = 0;
+  int coop = 0;  // cooperative launches supported
   cudaMemPool_t pool = nullptr;
   cudaError_t init_err = cudaSuccess;
 };
@@ -93,6 +122,8 @@ DeviceState *device_state(int dev) {
     if (e != cudaSuccess) { S.init_err = e; return; }
     uint64_t thr = UINT64_MAX;
     e = cudaMemPoolSetAttribute(S.pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (e != cudaSuccess) { S.init_err = e; return; }
+    e = cudaDeviceGetAttribute(&S.coop, cudaDevAttrCooperativeLaunch, dev);
     if (e != cudaSuccess) S.init_err = e;
   });
   return S.init_err == cudaSuccess ? &S : nullptr;
@@ -161,30 +192,31 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
 
   const Offsets off{offsets, nseg, heads ? 1 : 0, n};
 
-  // ---- tile sort: every segment of at most CAP elements -------------------
+  // ---- shapes ---------------------------------------------------------------
   using Cfg = typename TileFor<K, PAIRS>::Cfg;
-  auto tile_kernel = tile_sort_kernel<K, PAIRS, Cfg::NT, Cfg::KPT>;
+  auto tile_kernel = tile_sort_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
   static std::atomic<uint64_t> tile_attr_done{0};
   if (ensure_smem(tile_kernel, Cfg::kSmemBytes, tile_attr_done, dev) != cudaSuccess)
     return SEGSORT_ERR_CUDA;
+  const int64_t tiles = (n + Cfg::CAP - 1) / Cfg::CAP;
   const bool prof = g_prof_on.load(std::memory_order_relaxed);
   PhaseRecord rec;
-  if (prof) rec.t0 = prof_event(stream);
-  const int64_t tiles = (n + Cfg::CAP - 1) / Cfg::CAP;
-  tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off);
-  if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
-  if (prof) rec.t1 = prof_event(stream);
 
-  // ---- large segments ------------------------------------------------------
-  const WsLayout L = layout_for<K, PAIRS>(n);
-  if (L.total == 0) {
+  // ---- one tile: every segment fits, no workspace, one kernel ---------------
+  if (tiles == 1) {
+    if (prof) rec.t0 = prof_event(stream);
+    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     if (prof) {
+      rec.t1 = prof_event(stream);
       std::lock_guard<std::mutex> lk(g_prof_mu);
       g_prof_pending.push_back(rec);
     }
     return SEGSORT_OK;
   }
 
+  // ---- workspace ----------------------------------------------------------------
+  const WsLayout L = layout_for<K, PAIRS>(n);
   bool owned = false;
   unsigned char *base = static_cast<unsigned char *>(ws);
   if (base == nullptr) {
@@ -200,48 +232,67 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
 
   LargeWs<K> W;
   W.ctr = reinterpret_cast<uint32_t *>(base + L.ctr);
-  W.list = reinterpret_cast<int32_t *>(base + L.list);
+  W.jobs[0] = reinterpret_cast<int4 *>(base + L.jobs0);
+  W.jobs[1] = reinterpret_cast<int4 *>(base + L.jobs1);
   W.chunk_prefix = reinterpret_cast<int32_t *>(base + L.prefix);
   W.hist = reinterpret_cast<uint32_t *>(base + L.hist);
+  W.bstart = reinterpret_cast<int32_t *>(base + L.bstart);
+  W.digit = reinterpret_cast<int32_t *>(base + L.digit);
   W.status = reinterpret_cast<uint32_t *>(base + L.status);
+  W.desc = reinterpret_cast<int4 *>(base + L.desc);
+  W.entries = reinterpret_cast<int4 *>(base + L.entries);
+  W.half_first = reinterpret_cast<int32_t *>(base + L.half_first);
   W.tmp_keys = reinterpret_cast<K *>(base + L.tmp_keys);
   W.tmp_vals = PAIRS ? reinterpret_cast<uint32_t *>(base + L.tmp_vals) : nullptr;
-  W.max_large = L.max_large;
+  W.max_jobs = L.max_jobs;
   W.passes = L.passes;
   W.max_chunks = L.max_chunks;
+  W.max_entries = L.max_entries;
+  W.halves = L.halves;
 
   int rc = SEGSORT_OK;
-  if (prof) rec.l0 = prof_event(stream);
   do {
+    // ---- classify: half-tile -> first segment map, jobs for long segments ----
     if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess) {
       rc = SEGSORT_ERR_CUDA;
       break;
     }
-    const unsigned cls_blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 255) / 256);
-    large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), W);
-    large_scan_kernel<K><<<1, 1024, 0, stream>>>(W);
+    const unsigned cls_blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 1 + 255) / 256);
+    large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
 
-    static std::atomic<int> hist_occ[kMaxDevices];
-    static std::atomic<int> pass_occ[kMaxDevices];
-    const int ho = occupancy(large_hist_kernel<K>, kPassThreads, 0, hist_occ, dev);
-    const int po = occupancy(large_pass_kernel<K, PAIRS>, kPassThreads, 0, pass_occ, dev);
-    const int64_t hist_grid = std::min<int64_t>(L.max_chunks, static_cast<int64_t>(ho) * S->sms);
-    const int64_t pass_grid = std::min<int64_t>(L.max_chunks, static_cast<int64_t>(po) * S->sms);
-    large_hist_kernel<K><<<static_cast<unsigned>(hist_grid), kPassThreads, 0, stream>>>(keys, off, W);
-    for (int p = 0; p < L.passes; ++p) {
-      const bool even = (p & 1) == 0;
-      const K *sk = even ? keys : W.tmp_keys;
-      K *dk = even ? W.tmp_keys : keys;
-      const uint32_t *sv = PAIRS ? (even ? vals : W.tmp_vals) : nullptr;
-      uint32_t *dv = PAIRS ? (even ? W.tmp_vals : vals) : nullptr;
-      large_pass_kernel<K, PAIRS><<<static_cast<unsigned>(pass_grid), kPassThreads, 0, stream>>>(
-          sk, sv, dk, dv, off, W, p);
+    // ---- long segments: one cooperative kernel (returns at once if none) -----
+    using LS = LargeSmem<K, PAIRS, Cfg>;
+    auto large_kernel = large_sort_kernel<K, PAIRS, Cfg>;
+    static std::atomic<uint64_t> large_attr_done{0};
+    static std::atomic<int> large_occ[kMaxDevices];
+    if (!S->coop || ensure_smem(large_kernel, LS::kBytes, large_attr_done, dev) != cudaSuccess) {
+      rc = SEGSORT_ERR_CUDA;
+      break;
     }
+    const int lo = occupancy(large_kernel, kLThreads, LS::kBytes, large_occ, dev);
+    const unsigned large_grid = static_cast<unsigned>(lo * S->sms);
+    if (prof) rec.l0 = prof_event(stream);
+    {
+      K *kk = keys;
+      uint32_t *vv = vals;
+      void *args[] = {&kk, &vv, &W};
+      if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(large_kernel), dim3(large_grid),
+                                      dim3(kLThreads), args, LS::kBytes, stream) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+    }
+    if (prof) rec.l1 = prof_event(stream);
+
+    // ---- tile sort: every segment of at most CAP elements -----------------------
+    if (prof) rec.t0 = prof_event(stream);
+    tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
+        keys, vals, off, W.half_first);
+    if (prof) rec.t1 = prof_event(stream);
     if (cudaGetLastError() != cudaSuccess) rc = SEGSORT_ERR_CUDA;
   } while (false);
   if (prof) {
-    rec.l1 = prof_event(stream);
-    rec.large_launches = 3 + L.passes;  // classify, scan, hist, one per pass
+    rec.large_launches = 2;  // classify, the cooperative long-segment kernel
     std::lock_guard<std::mutex> lk(g_prof_mu);
     g_prof_pending.push_back(rec);
   }

@@ -88,27 +88,6 @@ __device__ __forceinline__ void raise_status(uint32_t bits) {
   atomicOr(&g_device_status, bits);
 }
 
-// Largest index j in [lo, hi] with off(j) <= limit (off non-decreasing and
-// off(lo) <= limit).
-__device__ __forceinline__ int64_t last_offset_le(const Offsets &off, int64_t lo,
-                                                  int64_t hi, int64_t limit) {
-  while (lo < hi) {
-    int64_t mid = (lo + hi + 1) >> 1;
-    if (off(mid) <= limit) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
-// First index s in [0, nseg] with off(s) >= pos (nseg if none).
-__device__ __forceinline__ int64_t first_offset_ge(const Offsets &off, int64_t pos) {
-  int64_t lo = 0, hi = off.nseg;
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if (off(mid) < pos) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
 __host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
 
 }  // namespace segsort

@@ -2,31 +2,39 @@
 // one CTA, entirely in shared memory and registers (one HBM read and one HBM
 // write per element).
 //
-// Work split.  CTA t owns the segments whose first element lies in the
-// nominal range [t*CAP, (t+1)*CAP).  It walks them in order and packs
-// consecutive segments into chunks of at most CAP elements (a binary search
-// over the offsets finds each chunk's last segment), so a chunk is a
-// contiguous element range made of whole segments.  Segments longer than CAP
-// are skipped here; the large-segment path sorts them.
+// Work split.  Half-tiles are CAP/2 elements wide; half_first[h] (written by
+// the classify kernel) is the first segment starting at or after h * CAP/2.
+// CTA t owns the segments starting in half-tiles 2t and 2t+1.  In a half-tile
+// every segment but the last is at most CAP/2 long (a longer one runs past
+// the half-tile's end, so nothing else starts after it there), so the short
+// segments of a half-tile span less than CAP elements and form one chunk; the
+// two halves' chunks are joined when they are contiguous and fit together.
+// A last segment longer than CAP/2 is a chunk of its own (up to CAP) or is
+// left to the large-segment path (longer than CAP).  A CTA therefore sorts at
+// most four chunks, found from three half_first entries and five offsets,
+// without any search.
 //
 // Chunk sort.  Every element becomes a composite word
 //     (segment start within the chunk, order bits of the key, chunk index)
 // compared as one unsigned integer.  Words are unique, so any sorting method
 // gives the stable per-segment order the reference's oracle produces with
 // std::stable_sort (src/bb_segsort/main.cu:152-173), and segments never mix
-// because the segment start is the most significant field.  The sort is a
-// merge sort: each thread sorts KPT words in registers with a bitonic network,
-// then log2(chunk / KPT) merge-path levels merge pairs of runs through
-// shared memory.  A pair whose runs are already in order (last word of the
-// first run <= first word of the second) is left as it is, so chunks of short
-// aligned segments skip the upper levels.  Values are staged once in shared
-// memory and gathered through the index field at the end.
+// because the segment start is the most significant field.  Segment starts
+// come from a shared-memory bitmask of segment heads and a block-wide running
+// maximum.  The sort is a merge sort: each thread sorts KPT words in registers
+// with a bitonic network, then log2(chunk / KPT) merge-path levels merge pairs
+// of runs through shared memory.  A pair whose runs are already in order (last
+// word of the first run <= first word of the second) is left as it is, so
+// chunks of short aligned segments skip the upper levels.  Values are staged
+// once in shared memory and gathered through the index field at the end.
 //
 // The reference sorts these lengths with one kernel per power-of-two length
 // bin (src/bb_segsort/bb_segsort.h:71-164, bins from bb_bin.h:54-100) using
 // unstable register networks; this kernel replaces that whole family and its
 // host round trip for the bin counts (bb_bin.h:46).
 #pragma once
+
+#include <cstring>
 
 #include "segsort_common.cuh"
 
@@ -48,6 +56,7 @@ template <> struct WordTraits<uint32_t> {
   }
   static __device__ __forceinline__ uint32_t bits(T w) { return static_cast<uint32_t>(w >> 16); }
   static __device__ __forceinline__ uint32_t index(T w) { return static_cast<uint32_t>(w) & 0xFFFFu; }
+  static __device__ __forceinline__ uint32_t seg(T w) { return static_cast<uint32_t>(w >> 48); }
   static __device__ __forceinline__ T maxv() { return ~0ull; }
   static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
   static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
@@ -78,6 +87,7 @@ template <> struct WordTraits<uint64_t> {
     return ((w.hi & 0xFFFFFFFFFFFFull) << 16) | (w.lo >> 16);
   }
   static __device__ __forceinline__ uint32_t index(T w) { return w.lo & 0xFFFFu; }
+  static __device__ __forceinline__ uint32_t seg(T w) { return static_cast<uint32_t>(w.hi >> 48); }
   static __device__ __forceinline__ T maxv() {
     T w;
     w.hi = ~0ull;
@@ -114,12 +124,14 @@ struct TileConfig {
   static constexpr int WSLOTS = CAP + CAP / WUNIT;
   // Output staging (keys then values), one padding slot per 32 elements.
   static constexpr int OSLOTS = CAP + CAP / 32;
+  static constexpr int HALF = CAP / 2;
   static constexpr size_t kWordBytes = static_cast<size_t>(WSLOTS) * sizeof(Word);
   static constexpr size_t kOutBytes =
       static_cast<size_t>(OSLOTS) * (sizeof(K) + (PAIRS ? sizeof(uint32_t) : 0));
   static constexpr size_t kMainBytes =
       ((kWordBytes > kOutBytes ? kWordBytes : kOutBytes) + 15) / 16 * 16;
-  static constexpr size_t kSmemBytes = kMainBytes + (PAIRS ? CAP * sizeof(uint32_t) : 0);
+  static constexpr size_t kValBytes = PAIRS ? CAP * sizeof(uint32_t) : 0;
+  static constexpr size_t kSmemBytes = kMainBytes + kValBytes;
 
   static __device__ __forceinline__ int wslot(int i) { return i + i / WUNIT; }
   static __device__ __forceinline__ int oslot(int i) { return i + (i >> 5); }
@@ -147,162 +159,388 @@ __device__ __forceinline__ void thread_sort(typename WT::T (&w)[KPT]) {
   }
 }
 
-template <typename K, bool PAIRS, int NT, int KPT>
-__global__ void __launch_bounds__(NT)
-tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off) {
-  using Cfg = TileConfig<K, PAIRS, NT, KPT>;
+// ---------------------------------------------------------------------------
+// Range copies between global memory and per-element callbacks: 16-byte
+// vector accesses for the aligned middle, UNROLL vectors per thread in flight,
+// scalar accesses for the unaligned head and tail.  The pair forms move keys
+// and values in one loop when both arrays share their 16-byte alignment.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ int align_head(const T *p, int m) {
+  const int h = static_cast<int>(((16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15) / sizeof(T));
+  return h < m ? h : m;
+}
+
+template <int NT, int UNROLL, typename T, typename F>
+__device__ __forceinline__ void load_range(const T *__restrict__ src, int m, F &&f) {
+  constexpr int V = 16 / static_cast<int>(sizeof(T));
+  const int tid = threadIdx.x;
+  const int head = align_head(src, m);
+  const int nvec = (m - head) / V;
+  const int tail0 = head + nvec * V;
+  if (tid < head) f(tid, __ldcs(src + tid));
+  const uint4 *pv = reinterpret_cast<const uint4 *>(src + head);
+  for (int k0 = tid; k0 < nvec; k0 += UNROLL * NT) {
+    uint4 v[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int k = k0 + u * NT;
+      if (k < nvec) v[u] = __ldcs(pv + k);
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int k = k0 + u * NT;
+      if (k < nvec) {
+        T e[V];
+        memcpy(e, &v[u], 16);
+#pragma unroll
+        for (int c = 0; c < V; ++c) f(head + k * V + c, e[c]);
+      }
+    }
+  }
+  if (tail0 + tid < m) f(tail0 + tid, __ldcs(src + tail0 + tid));
+}
+
+// 32-bit keys and 32-bit values with the same alignment: one loop.
+template <int NT, int UNROLL, typename K, typename FK, typename FV>
+__device__ __forceinline__ void load_pairs(const K *__restrict__ ks, const uint32_t *__restrict__ vs,
+                                           int m, FK &&fk, FV &&fv) {
+  static_assert(sizeof(K) == 4, "paired loop needs 32-bit keys");
+  const int head = align_head(ks, m);
+  if (head != align_head(vs, m)) {
+    load_range<NT, UNROLL>(ks, m, fk);
+    load_range<NT, UNROLL>(vs, m, fv);
+    return;
+  }
+  const int tid = threadIdx.x;
+  const int nvec = (m - head) / 4;
+  const int tail0 = head + nvec * 4;
+  if (tid < head) {
+    fk(tid, __ldcs(ks + tid));
+    fv(tid, __ldcs(vs + tid));
+  }
+  const uint4 *pk = reinterpret_cast<const uint4 *>(ks + head);
+  const uint4 *pvv = reinterpret_cast<const uint4 *>(vs + head);
+  for (int k0 = tid; k0 < nvec; k0 += UNROLL * NT) {
+    uint4 a[UNROLL], b[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int k = k0 + u * NT;
+      if (k < nvec) {
+        a[u] = __ldcs(pk + k);
+        b[u] = __ldcs(pvv + k);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int k = k0 + u * NT;
+      if (k < nvec) {
+        K e[4];
+        memcpy(e, &a[u], 16);
+        const int i = head + k * 4;
+        fk(i, e[0]); fk(i + 1, e[1]); fk(i + 2, e[2]); fk(i + 3, e[3]);
+        fv(i, b[u].x); fv(i + 1, b[u].y); fv(i + 2, b[u].z); fv(i + 3, b[u].w);
+      }
+    }
+  }
+  if (tail0 + tid < m) {
+    fk(tail0 + tid, __ldcs(ks + tail0 + tid));
+    fv(tail0 + tid, __ldcs(vs + tail0 + tid));
+  }
+}
+
+template <int NT, typename T, typename G>
+__device__ __forceinline__ void store_range(T *__restrict__ dst, int m, G &&g) {
+  constexpr int V = 16 / static_cast<int>(sizeof(T));
+  const int tid = threadIdx.x;
+  const int head = align_head(dst, m);
+  const int nvec = (m - head) / V;
+  const int tail0 = head + nvec * V;
+  if (tid < head) __stcs(dst + tid, g(tid));
+  uint4 *pv = reinterpret_cast<uint4 *>(dst + head);
+  for (int k = tid; k < nvec; k += NT) {
+    T e[V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) e[c] = g(head + k * V + c);
+    uint4 v;
+    memcpy(&v, e, 16);
+    __stcs(pv + k, v);
+  }
+  if (tail0 + tid < m) __stcs(dst + tail0 + tid, g(tail0 + tid));
+}
+
+// Exclusive running maximum over the threads of the CTA (-1 for thread 0).
+template <int NT>
+__device__ __forceinline__ int block_exclusive_max(int v, int *warp_s) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x = max(x, y);
+  }
+  int before = __shfl_up_sync(0xFFFFFFFFu, x, 1);
+  if (lane == 0) before = -1;
+  if (lane == 31) warp_s[warp] = x;
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < NT / 32; ++w)
+    if (w < warp) before = max(before, warp_s[w]);
+  __syncthreads();
+  return before;
+}
+
+// ---------------------------------------------------------------------------
+// Sorts one chunk of m <= CAP elements: reads src_keys/src_vals[0, m), writes
+// the result to dst_keys/dst_vals[0, m) (the same arrays for an in-place
+// sort; every read finishes before the first write).  `multi` says the chunk
+// holds more than one segment; then heads(set) is called by every thread and
+// must call set(p) for the local start p of each segment (any thread, any
+// order, repeats allowed).
+// ---------------------------------------------------------------------------
+template <typename Cfg, bool PAIRS, typename K, typename Heads>
+__device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *src_vals,
+                                           K *dst_keys, uint32_t *dst_vals, int m, bool multi,
+                                           Heads &&heads, unsigned char *smem, uint32_t *hb,
+                                           int *warp_s) {
   using Ord = typename Cfg::Ord;
   using WT = typename Cfg::WT;
   using Word = typename Cfg::Word;
-  constexpr int CAP = Cfg::CAP;
-
-  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NT = Cfg::NT;
+  constexpr int KPT = Cfg::KPT;
   Word *W = reinterpret_cast<Word *>(smem);
   K *KO = reinterpret_cast<K *>(smem);
   uint32_t *VO = reinterpret_cast<uint32_t *>(smem + Cfg::OSLOTS * sizeof(K));
   uint32_t *Vs = reinterpret_cast<uint32_t *>(smem + Cfg::kMainBytes);
-  __shared__ int64_t ctl[4];
-
   const int tid = threadIdx.x;
-  const int64_t n = off.n;
-  const int64_t t0 = static_cast<int64_t>(blockIdx.x) * CAP;
-  if (t0 >= n) return;
 
-  // Segments whose first element is in [t0, t0 + CAP): [s_cur, s_end).
-  int64_t s_cur = 0, s_end = 0;
-  if (tid == 0) {
-    s_cur = first_offset_ge(off, t0);
-    s_end = first_offset_ge(off, t0 + CAP);
+  if (multi) {
+    for (int i = tid; i < (m + 31) / 32; i += NT) hb[i] = 0;
+    __syncthreads();
+  }
+  // ---- load: keys -> words, values -> Vs, segment heads -> bitmask ----------
+  auto fk = [&](int i, K k) {
+    W[Cfg::wslot(i)] = WT::make(Ord::to_bits(k), static_cast<uint32_t>(i));
+  };
+  auto fv = [&](int i, uint32_t v) { Vs[i] = v; };
+  if constexpr (PAIRS && sizeof(K) == 4) {
+    load_pairs<NT, 4>(src_keys, src_vals, m, fk, fv);
+  } else {
+    load_range<NT, 4>(src_keys, m, fk);
+    if constexpr (PAIRS) load_range<NT, 4>(src_vals, m, fv);
+  }
+  if (multi) {
+    heads([&](int64_t p) {
+      if (p >= 0 && p < m) atomicOr(&hb[p >> 5], 1u << (p & 31));
+    });
+  }
+  __syncthreads();
+
+  // ---- blocked words + segment field ------------------------------------------
+  Word w[KPT];
+  const int base = tid * KPT;
+  if (multi) {
+    constexpr uint32_t kLow = KPT >= 32 ? 0xFFFFFFFFu : ((1u << KPT) - 1);
+    const uint32_t mask = base < m ? (hb[base >> 5] >> (base & 31)) & kLow : 0u;
+    const int mylast = mask ? base + 31 - __clz(mask) : -1;
+    const int carry = block_exclusive_max<NT>(mylast, warp_s);
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const int i = base + j;
+      if (i < m) {
+        const uint32_t mj = mask & ((2u << j) - 1u);
+        const int h = mj ? base + 31 - __clz(mj) : carry;
+        w[j] = WT::with_seg(W[Cfg::wslot(i)], static_cast<uint32_t>(h));
+      } else {
+        w[j] = WT::maxv();
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const int i = base + j;
+      w[j] = (i < m) ? W[Cfg::wslot(i)] : WT::maxv();
+    }
   }
 
-  while (true) {
-    if (tid == 0) {
-      int64_t a = 0, b = 0, lo = 0, hi = 0;
-      while (s_cur < s_end) {
-        a = off(s_cur);
-        const int64_t j = last_offset_le(off, s_cur, s_end, a + CAP);
-        if (j == s_cur) {  // longer than CAP: left to the large-segment path
-          ++s_cur;
-          continue;
-        }
-        lo = s_cur;
-        hi = j;
-        b = off(j);
-        s_cur = j;
-        break;
-      }
-      ctl[0] = a;
-      ctl[1] = b;
-      ctl[2] = lo;
-      ctl[3] = hi;
-    }
-    __syncthreads();
-    const int64_t a = ctl[0];
-    const int64_t seg_lo = ctl[2], seg_hi = ctl[3];
-    const int m = static_cast<int>(ctl[1] - a);
-    __syncthreads();
-    if (seg_hi == seg_lo) break;  // no more chunks
-    if (m <= 0) continue;          // only empty segments
-    const bool multi = (seg_hi - seg_lo) > 1;
+  thread_sort<WT, KPT>(w);
 
-    // ---- load: keys -> words (coalesced), values -> Vs -------------------
-    for (int i = tid; i < m; i += NT) {
-      W[Cfg::wslot(i)] = WT::make(Ord::to_bits(keys[a + i]), static_cast<uint32_t>(i));
-      if constexpr (PAIRS) Vs[i] = vals[a + i];
-    }
-    __syncthreads();
-
-    // ---- blocked words + segment field --------------------------------------
-    Word w[KPT];
-    const int base = tid * KPT;
-    int64_t next_begin = INT64_MAX, seg_begin = a;
-    if (multi && base < m) {
-      int64_t s = last_offset_le(off, seg_lo, seg_hi - 1, a + base);
-      seg_begin = off(s);
-      next_begin = off(s + 1);
-      // Walk forward past empty segments lazily inside the loop below.
-      int64_t s_walk = s;
-#pragma unroll
-      for (int j = 0; j < KPT; ++j) {
-        const int i = base + j;
-        if (i < m) {
-          while (a + i >= next_begin && s_walk + 1 < seg_hi) {
-            ++s_walk;
-            seg_begin = next_begin;
-            next_begin = off(s_walk + 1);
-          }
-          w[j] = WT::with_seg(W[Cfg::wslot(i)], static_cast<uint32_t>(seg_begin - a));
-        } else {
-          w[j] = WT::maxv();
-        }
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < KPT; ++j) {
-        const int i = base + j;
-        w[j] = (i < m) ? W[Cfg::wslot(i)] : WT::maxv();
-      }
-    }
-
-    thread_sort<WT, KPT>(w);
-
-    // ---- merge levels -------------------------------------------------------
-    for (int run = KPT; run < m; run <<= 1) {
-      __syncthreads();  // previous readers of W are done
+  // ---- merge levels ---------------------------------------------------------------
+  bool dirty = true;  // W does not hold this thread's current words
+  for (int run = KPT; run < m; run <<= 1) {
+    __syncthreads();  // previous readers of W are done
+    if (dirty) {
 #pragma unroll
       for (int j = 0; j < KPT; ++j) W[Cfg::wslot(base + j)] = w[j];
-      __syncthreads();
-      const int pair_threads = (2 * run) / KPT;
-      const int r = tid & (pair_threads - 1);
-      const int a_beg = (tid - r) * KPT;
-      const int a_end = a_beg + run;
-      const int b_end = a_end + run;
-      // Runs already in order: the merge is the concatenation, which is what
-      // this thread holds.
-      if (WT::le(W[Cfg::wslot(a_end - 1)], W[Cfg::wslot(a_end)])) continue;
-      const int diag = r * KPT;
-      int lo = diag > run ? diag - run : 0;
-      int hi = diag < run ? diag : run;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        const Word x = W[Cfg::wslot(a_beg + mid)];
-        const Word y = W[Cfg::wslot(a_end + diag - 1 - mid)];
-        if (WT::le(x, y)) lo = mid + 1; else hi = mid;
+    }
+    __syncthreads();
+    const int pair_threads = (2 * run) / KPT;
+    const int r = tid & (pair_threads - 1);
+    const int a_beg = (tid - r) * KPT;
+    const int a_end = a_beg + run;
+    const int b_end = a_end + run;
+    // Run A holds the sorted words of chunk positions [a_beg, a_end) and run B
+    // those of [a_end, b_end).  Segments are contiguous and the segment start
+    // is the top field, so every word of A is below every word of B except
+    // for the one segment that straddles position a_end.  Runs already in
+    // order: the merge is the concatenation, which is what this thread holds
+    // (and what W holds at its slots).
+    const Word x_last = W[Cfg::wslot(a_end - 1)];
+    const Word y_first = W[Cfg::wslot(a_end)];
+    if (WT::le(x_last, y_first)) {
+      dirty = false;
+      continue;
+    }
+    // Only the straddling segment's words [lo_p, hi_p) move.  They are a
+    // suffix of A and a prefix of B, so a thread whose own words (the run
+    // positions it holds) miss segment sg keeps them without searching.
+    int lo_p = a_beg, hi_p = b_end;
+    if (multi) {
+      const uint32_t sg = WT::seg(y_first);
+      const bool in_a = base < a_end;
+      if (WT::seg(in_a ? w[KPT - 1] : w[0]) != sg) {
+        dirty = false;
+        continue;
       }
-      int ai = a_beg + lo;
-      int bi = a_end + diag - lo;
-      Word av = ai < a_end ? W[Cfg::wslot(ai)] : WT::maxv();
-      Word bv = bi < b_end ? W[Cfg::wslot(bi)] : WT::maxv();
+      int l = a_beg, h = a_end - 1;  // first word of A in segment sg
+      while (l < h) {
+        const int mid = (l + h) >> 1;
+        if (WT::seg(W[Cfg::wslot(mid)]) < sg) l = mid + 1; else h = mid;
+      }
+      lo_p = l;
+      l = a_end + 1;
+      h = b_end;  // first word of B past segment sg
+      while (l < h) {
+        const int mid = (l + h) >> 1;
+        if (WT::seg(W[Cfg::wslot(mid)]) <= sg) l = mid + 1; else h = mid;
+      }
+      hi_p = l;
+    }
+    if (base + KPT <= lo_p || base >= hi_p) {
+      dirty = false;
+      continue;
+    }
+    dirty = true;
+    const int la = a_end - lo_p, lb = hi_p - a_end;
+    const int p0 = base > lo_p ? base : lo_p;
+    const int diag = p0 - lo_p;
+    int l = diag > lb ? diag - lb : 0;
+    int h = diag < la ? diag : la;
+    while (l < h) {
+      const int mid = (l + h) >> 1;
+      const Word x = W[Cfg::wslot(lo_p + mid)];
+      const Word y = W[Cfg::wslot(a_end + diag - 1 - mid)];
+      if (WT::le(x, y)) l = mid + 1; else h = mid;
+    }
+    int ai = lo_p + l;
+    int bi = a_end + diag - l;
+    Word av = ai < a_end ? W[Cfg::wslot(ai)] : WT::maxv();
+    Word bv = bi < hi_p ? W[Cfg::wslot(bi)] : WT::maxv();
 #pragma unroll
-      for (int j = 0; j < KPT; ++j) {
+    for (int j = 0; j < KPT; ++j) {
+      const int p = base + j;
+      if (p >= lo_p && p < hi_p) {
         const bool take_a = WT::le(av, bv);
         w[j] = take_a ? av : bv;
         ai += take_a;
         bi += !take_a;
         const int nx = take_a ? ai : bi;
-        const int lim = take_a ? a_end : b_end;
+        const int lim = take_a ? a_end : hi_p;
         const Word nv = nx < lim ? W[Cfg::wslot(nx)] : WT::maxv();
         av = take_a ? nv : av;
         bv = take_a ? bv : nv;
       }
     }
-    __syncthreads();
+  }
+  __syncthreads();
 
-    // ---- output: stage in shared memory, then coalesced stores -------------
+  // ---- output: stage in shared memory, then 16-byte stores -----------------------
 #pragma unroll
-    for (int j = 0; j < KPT; ++j) {
-      const int i = base + j;
-      if (i < m) {
-        KO[Cfg::oslot(i)] = Ord::from_bits(WT::bits(w[j]));
-        if constexpr (PAIRS) VO[Cfg::oslot(i)] = Vs[WT::index(w[j])];
+  for (int j = 0; j < KPT; ++j) {
+    const int i = base + j;
+    if (i < m) {
+      KO[Cfg::oslot(i)] = Ord::from_bits(WT::bits(w[j]));
+      if constexpr (PAIRS) VO[Cfg::oslot(i)] = Vs[WT::index(w[j])];
+    }
+  }
+  __syncthreads();
+  store_range<NT>(dst_keys, m, [&](int i) { return KO[Cfg::oslot(i)]; });
+  if constexpr (PAIRS) store_range<NT>(dst_vals, m, [&](int i) { return VO[Cfg::oslot(i)]; });
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// The kernel.  With half_first == null the problem is one tile (n <= CAP):
+// one chunk with every segment.
+// ---------------------------------------------------------------------------
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
+                 const int32_t *__restrict__ half_first) {
+  using Cfg = TileConfig<K, PAIRS, NT, KPT>;
+  constexpr int CAP = Cfg::CAP;
+  constexpr int64_t HALF = Cfg::HALF;
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int64_t chunk_s[4][3];  // a, lo, hi
+  __shared__ int32_t chunk_m[4];
+  __shared__ int nchunks_s;
+  __shared__ uint32_t hb[CAP / 32];
+  __shared__ int warp_s[NT / 32];
+
+  const int tid = threadIdx.x;
+  const int64_t n = off.n;
+  const int64_t nseg = off.nseg;
+  const int64_t t = blockIdx.x;
+  if (t * CAP >= n) return;
+
+  if (tid == 0) {
+    int nc = 0;
+    auto add = [&](int64_t lo, int64_t hi) {
+      if (hi <= lo) return;
+      const int64_t a = off(lo);
+      const int64_t m = off(hi) - a;
+      if (m <= 0 || m > CAP) return;
+      chunk_s[nc][0] = a;
+      chunk_s[nc][1] = lo;
+      chunk_s[nc][2] = hi;
+      chunk_m[nc] = static_cast<int32_t>(m);
+      ++nc;
+    };
+    if (half_first == nullptr) {
+      add(0, nseg);
+    } else {
+      auto clampi = [&](int64_t v, int64_t lo) { return v < lo ? lo : (v > nseg ? nseg : v); };
+      const int64_t h0 = clampi(__ldg(half_first + 2 * t), 0);
+      const int64_t h1 = clampi(__ldg(half_first + 2 * t + 1), h0);
+      const int64_t h2 = clampi(__ldg(half_first + 2 * t + 2), h1);
+      // A last segment of a half-tile longer than HALF is a chunk of its own.
+      const bool big_a = h1 > h0 && off(h1) - off(h1 - 1) > HALF;
+      const bool big_b = h2 > h1 && off(h2) - off(h2 - 1) > HALF;
+      const int64_t end_a = big_a ? h1 - 1 : h1;
+      const int64_t end_b = big_b ? h2 - 1 : h2;
+      if (!big_a && off(end_b) - off(h0) <= CAP) {
+        add(h0, end_b);  // both halves' short segments in one chunk
+      } else {
+        add(h0, end_a);
+        if (big_a) add(h1 - 1, h1);
+        add(h1, end_b);
       }
+      if (big_b) add(h2 - 1, h2);
     }
-    __syncthreads();
-    for (int i = tid; i < m; i += NT) {
-      keys[a + i] = KO[Cfg::oslot(i)];
-      if constexpr (PAIRS) vals[a + i] = VO[Cfg::oslot(i)];
-    }
-    __syncthreads();
+    nchunks_s = nc;
+  }
+  __syncthreads();
+  const int nc = nchunks_s;
+  for (int c = 0; c < nc; ++c) {
+    const int64_t a = chunk_s[c][0], lo = chunk_s[c][1], hi = chunk_s[c][2];
+    K *k = keys + a;
+    uint32_t *v = PAIRS ? vals + a : nullptr;
+    sort_chunk<Cfg, PAIRS>(k, v, k, v, chunk_m[c], hi - lo > 1,
+                           [&](auto &&set) {
+                             for (int64_t j = lo + tid; j < hi; j += NT) set(off(j) - a);
+                           },
+                           smem, hb, warp_s);
   }
 }
 
