@@ -133,6 +133,34 @@ int segsort_keys_u32_ws(uint32_t *d_keys, int64_t n, const int32_t *d_offsets,
                         size_t workspace_bytes, segsort_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Allocation-free form of segsort_pairs_u32.  No counterpart in the
+ * reference, whose drivers allocate device memory around every call
+ * (src/radixseg.cu:98-120, src/bb_segsort/bb_segsort.h:43-56).
+ *
+ * For callers that cannot allocate device memory where they sort: code whose
+ * device memory belongs to another allocator that already holds the device
+ * (a framework's caching allocator), real-time loops that must not block in,
+ * or fail on, an allocation once running, and code that must not fail with
+ * out-of-memory in mid-run.  The temporary storage is a fixed scratch array
+ * that is part of the library's device code, sized for n up to
+ * SEGSORT_NOALLOC_MAX_N uint32 key/value pairs (about 9.8 MiB); every GPU
+ * that loads the library holds it until the process exits.  The call makes
+ * no cudaMalloc, cudaFree or other allocating call.
+ *
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls share the one array, and every call
+ * clears what it needs at its start: calls that overlap on the GPU (other
+ * streams, or other host threads without ordering) race and corrupt each
+ * other's results, so order them on one stream.  n > SEGSORT_NOALLOC_MAX_N
+ * returns SEGSORT_ERR_TOO_LARGE before touching the GPU.
+ * ---------------------------------------------------------------------- */
+#define SEGSORT_NOALLOC_MAX_N 1048576
+int segsort_pairs_u32_noalloc(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                              const int32_t *d_offsets, int32_t nseg,
+                              segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Diagnostics.
  * segsort_device_status() synchronises the current device, returns
  * SEGSORT_OK or the first device-side error recorded since the last clear

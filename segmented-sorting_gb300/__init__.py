@@ -28,6 +28,7 @@ SEGSORT_ERR_TIMEOUT = -3
 SEGSORT_ERR_NO_MEMORY = -4
 SEGSORT_ERR_TOO_LARGE = -5
 SEGSORT_ERR_WORKSPACE = -6
+SEGSORT_NOALLOC_MAX_N = 1 << 20  # include/segsort.h
 
 KEY_TYPES = ("u32", "i32", "f32", "u64")
 
@@ -43,6 +44,7 @@ SIGNATURES = {
     "segsort_workspace_bytes": ([_I64, _I32, ctypes.c_int, ctypes.c_int], ctypes.c_size_t),
     "segsort_pairs_u32_ws": ([_P, _P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "segsort_keys_u32_ws": ([_P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "segsort_pairs_u32_noalloc": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int),
     "segsort_device_status": ([ctypes.c_int], ctypes.c_int),
     "segsort_error_string": ([ctypes.c_int], ctypes.c_char_p),
     "segsort_version": ([], ctypes.c_int),

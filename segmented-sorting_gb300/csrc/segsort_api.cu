@@ -53,9 +53,10 @@ struct WsLayout {
   int passes = 0;
 };
 
-size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+constexpr size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
-WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t cap, int64_t chunk) {
+constexpr WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t cap,
+                               int64_t chunk) {
   WsLayout L;
   if (n <= cap) return L;  // one tile: no workspace
   // Jobs of every level are longer than cap: at most n / (cap + 1) of them.
@@ -67,7 +68,7 @@ WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t cap, int64
   L.halves = 2 * ((n + cap - 1) / cap);
   L.passes = key_bytes;  // 8-bit digits
   size_t off = 0;
-  auto take = [&](size_t bytes) {
+  auto take = [&off](size_t bytes) {
     const size_t at = off;
     off = align256(off + bytes);
     return at;
@@ -103,8 +104,10 @@ struct DeviceState {
   std::once_flag once;
   int sms = 0;
   int coop = 0;  // cooperative launches supported
-  cudaMemPool_t pool = nullptr;
   cudaError_t init_err = cudaSuccess;
+  std::once_flag pool_once;  // the pool is created on the first internal allocation
+  cudaMemPool_t pool = nullptr;
+  cudaError_t pool_err = cudaSuccess;
 };
 DeviceState g_dev[kMaxDevices];
 
@@ -113,20 +116,26 @@ DeviceState *device_state(int dev) {
   DeviceState &S = g_dev[dev];
   std::call_once(S.once, [&] {
     cudaError_t e = cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) { S.init_err = e; return; }
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&S.coop, cudaDevAttrCooperativeLaunch, dev);
+    S.init_err = e;
+  });
+  return S.init_err == cudaSuccess ? &S : nullptr;
+}
+
+cudaMemPool_t device_pool(DeviceState &S, int dev) {
+  std::call_once(S.pool_once, [&] {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = dev;
-    e = cudaMemPoolCreate(&S.pool, &props);
-    if (e != cudaSuccess) { S.init_err = e; return; }
-    uint64_t thr = UINT64_MAX;
-    e = cudaMemPoolSetAttribute(S.pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    if (e != cudaSuccess) { S.init_err = e; return; }
-    e = cudaDeviceGetAttribute(&S.coop, cudaDevAttrCooperativeLaunch, dev);
-    if (e != cudaSuccess) S.init_err = e;
+    cudaError_t e = cudaMemPoolCreate(&S.pool, &props);
+    if (e == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      e = cudaMemPoolSetAttribute(S.pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    S.pool_err = e;
   });
-  return S.init_err == cudaSuccess ? &S : nullptr;
+  return S.pool_err == cudaSuccess ? S.pool : nullptr;
 }
 
 // Opt a kernel into more than 48 KB of dynamic shared memory once per device.
@@ -220,8 +229,10 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   bool owned = false;
   unsigned char *base = static_cast<unsigned char *>(ws);
   if (base == nullptr) {
-    if (cudaMallocFromPoolAsync(reinterpret_cast<void **>(&base), L.total, S->pool, stream) !=
-        cudaSuccess) {
+    cudaMemPool_t pool = device_pool(*S, dev);
+    if (pool == nullptr ||
+        cudaMallocFromPoolAsync(reinterpret_cast<void **>(&base), L.total, pool, stream) !=
+            cudaSuccess) {
       cudaGetLastError();
       return SEGSORT_ERR_NO_MEMORY;
     }
@@ -306,6 +317,35 @@ size_t workspace_bytes_for(int64_t n) {
   return layout_for<K, PAIRS>(n).total;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of the allocation-free entry point: the workspace of the largest
+// problem it accepts (SEGSORT_NOALLOC_MAX_N uint32 key/value pairs), as part of
+// the module's device image.  Host code cannot use the array's name as a
+// device address; its address is looked up once per device.
+constexpr int64_t kNoAllocMaxN = SEGSORT_NOALLOC_MAX_N;
+constexpr size_t kNoAllocBytes =
+    make_layout(kNoAllocMaxN, 4, 4, tile_cap<uint32_t>(), PassShape<uint32_t>::kChunk).total;
+static_assert(kNoAllocBytes > 0, "the no-allocation scratch must cover the long-segment path");
+
+struct NoAllocScratch {
+  std::once_flag once;
+  void *ptr = nullptr;
+  cudaError_t err = cudaSuccess;
+};
+NoAllocScratch g_noalloc[kMaxDevices];
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+// Device address of the scratch array on `dev`, which must be the current
+// device: looked up on the first call per device, then cached.
+void *noalloc_scratch(int dev) {
+  NoAllocScratch &S = g_noalloc[dev];
+  std::call_once(S.once, [&] { S.err = cudaGetSymbolAddress(&S.ptr, g_noalloc_scratch); });
+  return S.err == cudaSuccess ? S.ptr : nullptr;
+}
 }  // namespace
 }  // namespace segsort
 
@@ -374,6 +414,20 @@ int segsort_keys_u32_ws(uint32_t *k, int64_t n, const int32_t *o, int32_t ns, vo
                         size_t ws_bytes, segsort_stream_t s) {
   if (ws == nullptr && segsort_workspace_bytes(n, ns, 4, 0) != 0) return SEGSORT_ERR_WORKSPACE;
   return sort_impl<uint32_t, false>(k, nullptr, n, o, ns, false, ws, ws_bytes, SEGSORT_ST(s));
+}
+
+int segsort_pairs_u32_noalloc(uint32_t *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                              segsort_stream_t s) {
+  if (n < 0 || ns < 0) return SEGSORT_ERR_INVALID_ARG;
+  if (n > segsort::kNoAllocMaxN) return SEGSORT_ERR_TOO_LARGE;
+  if (n == 0 || ns == 0) return SEGSORT_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= segsort::kMaxDevices)
+    return SEGSORT_ERR_CUDA;
+  void *scratch = segsort::noalloc_scratch(dev);
+  if (scratch == nullptr) return SEGSORT_ERR_CUDA;
+  return sort_impl<uint32_t, true>(k, v, n, o, ns, false, scratch, segsort::kNoAllocBytes,
+                                   SEGSORT_ST(s));
 }
 
 int segsort_device_status(int clear) {
