@@ -40,11 +40,11 @@ namespace segsort {
 
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
-constexpr int kLThreads = 256;  // CTA size: one thread per digit in the digit loops
+constexpr int kLThreads = 512;  // CTA size; threads [0, kRadix) own one digit each in the digit loops
 constexpr int kLWarps = kLThreads / 32;
 
-// Keys per thread and per chunk of the scatter: 4096 keys for 32-bit keys,
-// 2048 for 64-bit keys.
+// Keys per thread and per chunk of the scatter: 8192 keys for 32-bit keys,
+// 4096 for 64-bit keys.
 template <typename K>
 struct PassShape {
   static constexpr int kItems = sizeof(K) == 4 ? 16 : 8;
@@ -68,7 +68,7 @@ enum : int {
   kCtrWords = 16,
 };
 
-enum : int { kEntrySort = 0, kEntryCopy = 1 };
+enum : int { kEntrySort = 0, kEntryCopy = 1, kEntryDirect = 2 };
 constexpr int32_t kDigitUnset = -2;  // digit[] before the scatter wrote it
 constexpr int32_t kDigitNone = -1;   // no remaining byte varies: keys are equal
 
@@ -83,7 +83,8 @@ struct LargeWs {
   int32_t *digit;         // [max_jobs] byte the job was split on
   uint32_t *status;       // [max_chunks][kRadix] look-back words
   int4 *desc;             // [max_chunks] chunk begin, job end, job index, job begin
-  int4 *entries;          // [max_entries] {job, d0, d1, sort} or {begin, len, 0, copy}
+  int4 *entries;          // [max_entries] {job, d0, d1, sort}, {begin, len, 0, copy} or
+                          // {begin, len, 0, direct}
   int32_t *half_first;    // [halves + 1] first segment starting at or after h * CAP/2
   K *tmp_keys;            // [n]
   uint32_t *tmp_vals;     // [n]
@@ -206,9 +207,9 @@ constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
 template <typename K, bool PAIRS, typename Cfg>
 struct LargeSmem {
   static constexpr int kChunk = PassShape<K>::kChunk;
-  // Histogram tables: one per warp for 32-bit keys, one per warp pair for
+  // Histogram tables shared by groups of warps: 8 for 32-bit keys, 4 for
   // 64-bit keys (32 KB either way).
-  static constexpr int kHistTables = sizeof(typename KeyOrder<K>::Bits) == 4 ? kLWarps : kLWarps / 2;
+  static constexpr int kHistTables = sizeof(typename KeyOrder<K>::Bits) == 4 ? 8 : 4;
   static constexpr size_t kHist = kHistTables * sizeof(typename KeyOrder<K>::Bits) * kRadix * 4;
   static constexpr size_t kScatter = kLWarps * kRadix * 4   // per-warp digit counts
                                      + 2 * kRadix * 4       // chunk offsets, deltas
@@ -220,7 +221,7 @@ struct LargeSmem {
 
 // ---------------------------------------------------------------------------
 template <typename K, bool PAIRS, typename Cfg>
-__global__ void __launch_bounds__(kLThreads, 2)
+__global__ void __launch_bounds__(kLThreads, 1)
 large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> ws) {
   using Ord = KeyOrder<K>;
   using Bits = typename Ord::Bits;
@@ -268,7 +269,8 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         if (j < nj) {
           const int4 jb = jobs[j];
           const int64_t len = jb.y > jb.x ? jb.y - jb.x : 0;
-          v = static_cast<uint32_t>((len + kChunk - 1) / kChunk);
+          // Level-0 jobs that fit the bucket sort are sorted directly.
+          v = (level == 0 && len <= CAP) ? 0u : static_cast<uint32_t>((len + kChunk - 1) / kChunk);
         }
         const uint32_t ex = block_exclusive_sum(v, warp_tmp);
         const uint64_t e64 = carry_s + ex;
@@ -399,7 +401,7 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         // Highest byte with two or more non-empty digits.
         int D = kDigitNone;
         for (int q = min(jobs[j].z, passes) - 1; q >= 0; --q) {
-          if (__syncthreads_count(jh[q * kRadix + tid] != 0) > 1) {
+          if (__syncthreads_count(tid < kRadix && jh[q * kRadix + tid] != 0) > 1) {
             D = q;
             break;
           }
@@ -439,56 +441,61 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         }
         __syncthreads();
 
-        // Per digit: warp prefixes, chunk total, look-back, global offsets.
+        // Per digit (threads [0, kRadix)): warp prefixes, chunk total,
+        // look-back, global offsets.
         const int d = tid;
-        uint32_t tot = 0;
+        const bool owner = d < kRadix;
+        uint32_t tot = 0, excl = 0, hcount = 0;
+        if (owner) {
 #pragma unroll
-        for (int w = 0; w < kLWarps; ++w) {
-          const uint32_t x = whist[w * kRadix + d];
-          whist[w * kRadix + d] = tot;
-          tot += x;
-        }
-        uint32_t *st = ws.status + static_cast<size_t>(t) * kRadix;
-        uint32_t excl = 0;
-        if (c == 0) {
-          st_volatile(st + d, kFlagInclusive | tot);
-        } else {
-          st_volatile(st + d, kFlagAggregate | tot);
-          const int64_t q_first = t - c;  // the job's first chunk (always inclusive)
-          int64_t q = t - 1;
-          while (true) {
-            if (q < q_first) {  // unreachable: chunk q_first publishes an inclusive value
-              raise_status(kStatusTimeout);
-              break;
-            }
-            const uint32_t *qs = ws.status + static_cast<size_t>(q) * kRadix;
-            uint32_t v = ld_volatile(qs + d);
-            int spins = 0;
-            while ((v >> 30) == 0 && spins < kLookbackSpinLimit) {
-              if (spins > 64) __nanosleep(64);
-              ++spins;
-              v = ld_volatile(qs + d);
-            }
-            if ((v >> 30) == 0) {
-              raise_status(kStatusTimeout);
-              break;
-            }
-            excl += v & kValueMask;
-            if (v & kFlagInclusive) break;
-            --q;
+          for (int w = 0; w < kLWarps; ++w) {
+            const uint32_t x = whist[w * kRadix + d];
+            whist[w * kRadix + d] = tot;
+            tot += x;
           }
-          st_volatile(st + d, kFlagInclusive | ((excl + tot) & kValueMask));
+          uint32_t *st = ws.status + static_cast<size_t>(t) * kRadix;
+          if (c == 0) {
+            st_volatile(st + d, kFlagInclusive | tot);
+          } else {
+            st_volatile(st + d, kFlagAggregate | tot);
+            const int64_t q_first = t - c;  // the job's first chunk (always inclusive)
+            int64_t q = t - 1;
+            while (true) {
+              if (q < q_first) {  // unreachable: chunk q_first publishes an inclusive value
+                raise_status(kStatusTimeout);
+                break;
+              }
+              const uint32_t *qs = ws.status + static_cast<size_t>(q) * kRadix;
+              uint32_t v = ld_volatile(qs + d);
+              int spins = 0;
+              while ((v >> 30) == 0 && spins < kLookbackSpinLimit) {
+                if (spins > 64) __nanosleep(64);
+                ++spins;
+                v = ld_volatile(qs + d);
+              }
+              if ((v >> 30) == 0) {
+                raise_status(kStatusTimeout);
+                break;
+              }
+              excl += v & kValueMask;
+              if (v & kFlagInclusive) break;
+              --q;
+            }
+            st_volatile(st + d, kFlagInclusive | ((excl + tot) & kValueMask));
+          }
+          hcount = jh[D * kRadix + d];
         }
         const uint32_t boff = block_exclusive_sum(tot, warp_tmp);
-        const uint32_t hcount = jh[D * kRadix + d];
         const uint32_t dbase = block_exclusive_sum(hcount, warp_tmp);
-        boff_s[d] = boff;
-        delta_s[d] = static_cast<int32_t>(dbase + excl) - static_cast<int32_t>(boff);
-        if (c == 0) {  // the job's bucket starts, for the planning phase
-          int32_t *bs = ws.bstart + static_cast<size_t>(j) * (kRadix + 1);
-          bs[d] = static_cast<int32_t>(dbase);
-          if (d == kRadix - 1) bs[kRadix] = static_cast<int32_t>(dbase + hcount);
-          if (d == 0) ws.digit[j] = D;
+        if (owner) {
+          boff_s[d] = boff;
+          delta_s[d] = static_cast<int32_t>(dbase + excl) - static_cast<int32_t>(boff);
+          if (c == 0) {  // the job's bucket starts, for the planning phase
+            int32_t *bs = ws.bstart + static_cast<size_t>(j) * (kRadix + 1);
+            bs[d] = static_cast<int32_t>(dbase);
+            if (d == kRadix - 1) bs[kRadix] = static_cast<int32_t>(dbase + hcount);
+            if (d == 0) ws.digit[j] = D;
+          }
         }
         __syncthreads();
 
@@ -525,6 +532,13 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
       int32_t *bs_s = reinterpret_cast<int32_t *>(smem) + warp * (kRadix + 1);
       for (int64_t j = static_cast<int64_t>(blockIdx.x) * kLWarps + warp; j < nj; j += G * kLWarps) {
         const int4 jb = jobs[j];
+        if (level == 0 && jb.y - jb.x <= CAP) {  // fits the bucket sort: sorted in place
+          if (lane == 0) {
+            const uint32_t k = atomicAdd(&ws.ctr[kCtrBuckets], 1u);
+            if (k < ws.max_entries) ws.entries[k] = make_int4(jb.x, jb.y - jb.x, 0, kEntryDirect);
+          }
+          continue;
+        }
         const int32_t D = ld_volatile(ws.digit + j);
         if (D == kDigitUnset) continue;  // not scattered (malformed offsets only)
         if (D >= 0) {
@@ -630,6 +644,15 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
           next_t = atomicAdd(&ws.ctr[kCtrBucketTicket], 1u);
           if (next_t < nent) next_e = ws.entries[next_t];
         }
+        if (en.w == kEntryDirect) {
+          const int64_t a = en.x;
+          const int m = en.y;
+          if (m > 0 && m <= CAP)
+            sort_chunk<Cfg, PAIRS>(keys + a, PAIRS ? vals + a : nullptr, keys + a,
+                                   PAIRS ? vals + a : nullptr, m, false, [](auto &&) {}, smem,
+                                   hb, warp_s);
+          continue;
+        }
         if (en.w == kEntryCopy) {
           const int64_t a = en.x;
           const int m = en.y;
@@ -646,11 +669,12 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         const int64_t a = jb.x + s0;
         const int64_t m = static_cast<int64_t>(bs[d1]) - s0;
         if (m <= 0 || m > CAP || a < jb.x || a + m > jb.y) continue;  // malformed only
+        // The buckets of one job are ordered by their digit, the highest byte
+        // that varies in the job, so sorting the chunk as one segment by the
+        // whole key sorts every bucket in it.
         sort_chunk<Cfg, PAIRS>(dst_k + a, PAIRS ? dst_v + a : nullptr, keys + a,
-                               PAIRS ? vals + a : nullptr, static_cast<int>(m), d1 - d0 > 1,
-                               [&](auto &&set) {
-                                 for (int d = d0 + tid; d < d1; d += kLThreads) set(bs[d] - s0);
-                               },
+                               PAIRS ? vals + a : nullptr, static_cast<int>(m), false,
+                               [](auto &&) {},
                                smem, hb, warp_s);
       }
     }

@@ -40,6 +40,13 @@ constexpr int64_t tile_cap() {
   return TileFor<K, false>::Cfg::CAP;
 }
 
+// Bucket-sort shape of the long-segment kernel: its 512-thread CTAs sort
+// chunks of 8192 (32-bit keys) or 4096 (64-bit keys) elements.
+template <typename K, bool PAIRS>
+struct LargeFor {
+  using Cfg = TileConfig<K, PAIRS, kLThreads, sizeof(K) == 4 ? 16 : 8>;
+};
+
 // ---------------------------------------------------------------------------
 // Workspace layout (every region 256-byte aligned).
 struct WsLayout {
@@ -272,8 +279,9 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
 
     // ---- long segments: one cooperative kernel (returns at once if none) -----
-    using LS = LargeSmem<K, PAIRS, Cfg>;
-    auto large_kernel = large_sort_kernel<K, PAIRS, Cfg>;
+    using LCfg = typename LargeFor<K, PAIRS>::Cfg;
+    using LS = LargeSmem<K, PAIRS, LCfg>;
+    auto large_kernel = large_sort_kernel<K, PAIRS, LCfg>;
     static std::atomic<uint64_t> large_attr_done{0};
     static std::atomic<int> large_occ[kMaxDevices];
     if (!S->coop || ensure_smem(large_kernel, LS::kBytes, large_attr_done, dev) != cudaSuccess) {

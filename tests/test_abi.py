@@ -79,7 +79,7 @@ def test_workspace_sizes(pkg):
     ws_keys = L.segsort_workspace_bytes(n, 1, 4, 0)
     # the ping-pong copy of the keys (and values) dominates
     assert ws_pairs >= 8 * n and ws_keys >= 4 * n and ws_pairs - ws_keys >= 4 * n
-    assert ws_pairs < 12 * n
+    assert ws_pairs < 11 * n
     assert L.segsort_workspace_bytes(n, 1, 8, 4) >= 12 * n
 
 
