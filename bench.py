@@ -63,6 +63,8 @@ def parse_args():
     p.add_argument("--cpu-sample-log", type=int, default=22)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the 64-instance batch")
+    p.add_argument("--no-configs", action="store_true", help="skip the other workloads")
     return p.parse_args()
 
 
@@ -208,6 +210,154 @@ def run_reference(args) -> None:
         "e2e": {"value": value, "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+BATCH_WORKLOAD = ("64 independent instances, n log-uniform in [2^16, 2^24], segment lengths "
+                  "equal (length log-uniform in [2, 2^16]) or lognormal(4, 2.5), keys u32/u64/f32 "
+                  "in turn, uint32 values = index")
+_TORCH_KEY = {"u32": "int32", "i32": "int32", "f32": "float32", "u64": "int64"}
+
+
+def _timed(stream, fn, restore, warmup: int, steps: int) -> list[float]:
+    """CUDA-event ms of fn() per step; restore() (untimed) refreshes the inputs."""
+    import torch
+    out = []
+    for s in range(warmup + steps):
+        restore()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        if s >= warmup:
+            out.append((a, b))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in out]
+
+
+def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
+    """The 64-instance mixed batch: one replay of a batch plan (one CUDA graph)
+    against the same 64 instances as back-to-back plain calls, on fresh copies
+    of the inputs every step (1.7 GB of pairs: above L2)."""
+    import torch
+    L = pkg.lib()
+    st = stream.cuda_stream
+    specs = inst.batch_specs()
+    rows = []
+    for s in specs:
+        off = torch.from_numpy(inst.batch_offsets(s)).to(dev)
+        keys = inst.device_typed_keys(s["n"], s["seed"], s["key_type"], device=dev)
+        vals = torch.arange(s["n"], dtype=torch.int32, device=dev)
+        rows.append({"spec": s, "off": off, "k0": keys, "v0": vals,
+                     "k": torch.empty_like(keys), "v": torch.empty_like(vals)})
+    total = sum(s["n"] for s in specs)
+
+    def restore():
+        for r in rows:
+            r["k"].copy_(r["k0"])
+            r["v"].copy_(r["v0"])
+
+    def plain():
+        for r in rows:
+            s = r["spec"]
+            rc = getattr(L, f"segsort_pairs_{s['key_type']}")(
+                r["k"].data_ptr(), r["v"].data_ptr(), s["n"], r["off"].data_ptr(),
+                r["off"].numel() - 1, st)
+            if rc != 0:
+                raise pkg.SegsortError(rc, "plain call")
+
+    items = (pkg.BatchItem * len(rows))(*[
+        pkg.BatchItem(pkg.KEY_TYPE_CODES[r["spec"]["key_type"]], 0, r["k"].data_ptr(),
+                      r["v"].data_ptr(), r["spec"]["n"], r["off"].data_ptr(),
+                      r["off"].numel() - 1, 0) for r in rows])
+
+    def one_shot():
+        rc = L.segsort_pairs_batch(items, len(rows), st)
+        if rc != 0:
+            raise pkg.SegsortError(rc, "segsort_pairs_batch")
+
+    plan = ctypes.c_void_p()
+    rc = L.segsort_batch_plan_create(items, len(rows), ctypes.byref(plan))
+    if rc != 0:
+        raise pkg.SegsortError(rc, "segsort_batch_plan_create")
+
+    def replay():
+        rc = L.segsort_batch_plan_launch(plan, st)
+        if rc != 0:
+            raise pkg.SegsortError(rc, "segsort_batch_plan_launch")
+
+    try:
+        t_plain = _timed(stream, plain, restore, warmup, steps)
+        ref = [(r["k"].clone(), r["v"].clone()) for r in rows]
+        t_one = _timed(stream, one_shot, restore, warmup, steps)
+        t_plan = _timed(stream, replay, restore, warmup, steps)
+        identical = all(torch.equal(r["k"], k) and torch.equal(r["v"], v)
+                        for r, (k, v) in zip(rows, ref))
+        ws = L.segsort_batch_plan_workspace_bytes(plan)
+    finally:
+        L.segsort_batch_plan_destroy(plan)
+    if pkg.device_status() != 0:
+        raise RuntimeError("device status reports a bounded wait that gave up")
+    if not identical:
+        raise RuntimeError("batched output differs from the plain calls")
+    med = {k: statistics.median(v) for k, v in
+           (("plain", t_plain), ("one_shot", t_one), ("plan", t_plan))}
+    types = sorted({s["key_type"] for s in specs})
+    return {
+        "workload": BATCH_WORKLOAD, "instances": len(specs), "keys": total,
+        "key_types": {t: sum(1 for s in specs if s["key_type"] == t) for t in types},
+        "plain_ms": round(med["plain"], 4), "one_shot_ms": round(med["one_shot"], 4),
+        "plan_ms": round(med["plan"], 4),
+        "plain_gkeys_s": round(total / (med["plain"] * 1e-3) / 1e9, 3),
+        "plan_gkeys_s": round(total / (med["plan"] * 1e-3) / 1e9, 3),
+        "speedup_plan_vs_plain": round(med["plain"] / med["plan"], 3),
+        "plan_p99_ms": round(float(np.percentile(t_plan, 99)), 4),
+        "identical_to_plain": identical, "plan_workspace_bytes": ws, "steps": steps,
+        "launches": {"plain": 3 * len(specs), "plan_graph": 3 * len(types)},
+    }
+
+
+def bench_configs(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
+    """The plain call on the other single-instance workloads: 2^20 keys-only
+    (1024 x 1024, keys < 2^31) and 2^25 pairs with lognormal segment lengths
+    (uniform and Zipf(1.1) keys)."""
+    import torch
+    L = pkg.lib()
+    st = stream.cuda_stream
+    out = {}
+    n1 = 1 << 20
+    k0 = inst.device_uniform_keys(n1, seed=1, bits=31, device=dev)
+    o1 = torch.from_numpy(inst.equal_offsets(n1, 1024)).to(dev)
+    k = torch.empty_like(k0)
+    t = _timed(stream, lambda: L.segsort_keys_u32(k.data_ptr(), n1, o1.data_ptr(), 1024, st),
+               lambda: k.copy_(k0), warmup, steps)
+    ms = statistics.median(t)
+    out["keys_2e20_1024x1024"] = {"ms": round(ms, 5), "gkeys_s": round(n1 / (ms * 1e-3) / 1e9, 3)}
+    n3 = 1 << 25
+    o3n = inst.lognormal_offsets(n3, seed=1)
+    o3 = torch.from_numpy(o3n).to(dev)
+    lens = np.diff(o3n)
+    v0 = torch.arange(n3, dtype=torch.int32, device=dev)
+    for name, keys in (("uniform", inst.device_uniform_keys(n3, seed=1, bits=32, device=dev)),
+                       ("zipf", torch.from_numpy(inst.zipf_keys(n3, seed=1).view(np.int32)).to(dev))):
+        kk, vv = torch.empty_like(keys), torch.empty_like(v0)
+
+        def restore():
+            kk.copy_(keys)
+            vv.copy_(v0)
+
+        t = _timed(stream, lambda: L.segsort_pairs_u32(kk.data_ptr(), vv.data_ptr(), n3,
+                                                       o3.data_ptr(), len(o3n) - 1, st),
+                   restore, warmup, steps)
+        ms = statistics.median(t)
+        out[f"pairs_2e25_lognormal_{name}"] = {
+            "ms": round(ms, 4), "gkeys_s": round(n3 / (ms * 1e-3) / 1e9, 3),
+            "segments": int(len(lens)), "empty": int((lens == 0).sum()),
+            "max_len": int(lens.max())}
+    if pkg.device_status() != 0:
+        raise RuntimeError("device status reports a bounded wait that gave up")
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -389,6 +539,10 @@ def run_ours(args) -> None:
         if not (np.all(got_k[:-1] <= got_k[1:]) and np.array_equal(src_k[got_v], got_k)):
             raise RuntimeError("end-to-end read-back is not the sorted segment")
 
+    # ---- the batched form and the other workloads ---------------------------
+    batched = None if args.no_batched else bench_batched(pkg, inst, dev, stream, 2, 5)
+    configs = None if args.no_configs else bench_configs(pkg, inst, dev, stream, 3, 10)
+
     # ---- CPU baseline (rank 0) ----------------------------------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -414,6 +568,7 @@ def run_ours(args) -> None:
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(), "per_len": per_len,
+            "batched": batched, "configs": configs,
         }), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -161,6 +161,54 @@ int segsort_pairs_u32_noalloc(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
                               segsort_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Batched form: many independent instances, each with its own keys, uint32
+ * values and offsets, sorted by one launch of each kernel per key type
+ * instead of one sequence of launches per instance.  No counterpart in the
+ * reference, which sorts one instance per program; it replaces the
+ * reference's launch loops over streams (src/newthrust.cu:137-157) and its
+ * per-bin streams (src/bb_segsort/bb_segsort.h:60-61) as the way to keep the
+ * GPU busy with many small problems.
+ *
+ * Every item is the argument list of one segsort_pairs_<type> call
+ * (heads = 1: the segsort_pairs_u32_heads convention).  Items must not
+ * overlap in memory.  The result of every item is bit for bit the result of
+ * its own plain call.  Limits: each item n < 2^30, and the items of one key
+ * type together fewer than 2^31 elements (SEGSORT_ERR_TOO_LARGE).
+ * ---------------------------------------------------------------------- */
+#define SEGSORT_KEY_U32 0
+#define SEGSORT_KEY_I32 1
+#define SEGSORT_KEY_F32 2
+#define SEGSORT_KEY_U64 3
+
+typedef struct segsort_batch_item {
+  int32_t key_type; /* SEGSORT_KEY_*                               */
+  int32_t heads;    /* 1: d_offsets holds nseg heads, end = n       */
+  void *d_keys;     /* n keys of key_type                           */
+  uint32_t *d_vals; /* n values                                     */
+  int64_t n;
+  const int32_t *d_offsets;
+  int32_t nseg;
+  int32_t reserved; /* 0                                            */
+} segsort_batch_item;
+
+/* One-shot: enqueues the batch on `stream` (workspace from the library's
+ * pool, no host synchronisation). */
+int segsort_pairs_batch(const segsort_batch_item *items, int32_t count,
+                        segsort_stream_t stream);
+
+/* Plan: validates the items once, allocates the workspace, and captures the
+ * whole batch into one CUDA graph.  Each launch replays the graph on
+ * `stream`: it sorts whatever the items' buffers hold at that time, at the
+ * same addresses.  Launches of one plan must not overlap (they share its
+ * workspace): order them on one stream. */
+typedef struct segsort_batch_plan_s *segsort_batch_plan;
+int segsort_batch_plan_create(const segsort_batch_item *items, int32_t count,
+                              segsort_batch_plan *plan);
+int segsort_batch_plan_launch(segsort_batch_plan plan, segsort_stream_t stream);
+size_t segsort_batch_plan_workspace_bytes(segsort_batch_plan plan);
+void segsort_batch_plan_destroy(segsort_batch_plan plan);
+
+/* ------------------------------------------------------------------------
  * Diagnostics.
  * segsort_device_status() synchronises the current device, returns
  * SEGSORT_OK or the first device-side error recorded since the last clear

@@ -31,6 +31,15 @@ SEGSORT_ERR_WORKSPACE = -6
 SEGSORT_NOALLOC_MAX_N = 1 << 20  # include/segsort.h
 
 KEY_TYPES = ("u32", "i32", "f32", "u64")
+KEY_TYPE_CODES = {"u32": 0, "i32": 1, "f32": 2, "u64": 3}  # SEGSORT_KEY_* of include/segsort.h
+
+
+class BatchItem(ctypes.Structure):
+    """segsort_batch_item of include/segsort.h."""
+    _fields_ = [("key_type", ctypes.c_int32), ("heads", ctypes.c_int32),
+                ("d_keys", ctypes.c_void_p), ("d_vals", ctypes.c_void_p),
+                ("n", ctypes.c_int64), ("d_offsets", ctypes.c_void_p),
+                ("nseg", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 # Every symbol include/segsort.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
@@ -45,6 +54,11 @@ SIGNATURES = {
     "segsort_pairs_u32_ws": ([_P, _P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "segsort_keys_u32_ws": ([_P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "segsort_pairs_u32_noalloc": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int),
+    "segsort_pairs_batch": ([ctypes.POINTER(BatchItem), _I32, _P], ctypes.c_int),
+    "segsort_batch_plan_create": ([ctypes.POINTER(BatchItem), _I32, ctypes.POINTER(_P)], ctypes.c_int),
+    "segsort_batch_plan_launch": ([_P, _P], ctypes.c_int),
+    "segsort_batch_plan_workspace_bytes": ([_P], ctypes.c_size_t),
+    "segsort_batch_plan_destroy": ([_P], None),
     "segsort_device_status": ([ctypes.c_int], ctypes.c_int),
     "segsort_error_string": ([ctypes.c_int], ctypes.c_char_p),
     "segsort_version": ([], ctypes.c_int),
@@ -180,3 +194,57 @@ def profile_read(reset: bool = True) -> dict:
                                       ctypes.byref(nl), 1 if reset else 0), "profile_read")
     return {"tile_ms": t.value, "large_ms": l.value, "tile_launches": nt.value,
             "large_launches": nl.value}
+
+
+# ---------------------------------------------------------------------------
+# Batched form.
+# ---------------------------------------------------------------------------
+def batch_items(instances) -> ctypes.Array:
+    """ctypes array of segsort_batch_item from (keys, values, offsets, key_type)
+    tuples of CUDA tensors (CSR offsets: nseg + 1 int32 entries)."""
+    import torch
+    arr = (BatchItem * len(instances))()
+    for i, (keys, values, offsets, key_type) in enumerate(instances):
+        if not (keys.is_cuda and values.is_cuda and offsets.is_cuda):
+            raise ValueError("batch tensors must be CUDA tensors")
+        if offsets.dtype != torch.int32 or values.element_size() != 4:
+            raise TypeError("offsets must be int32 and values 32-bit")
+        if values.numel() != keys.numel():
+            raise ValueError("values must hold one element per key")
+        arr[i] = BatchItem(KEY_TYPE_CODES[key_type], 0, keys.data_ptr(), values.data_ptr(),
+                           keys.numel(), offsets.data_ptr(), offsets.numel() - 1, 0)
+    return arr
+
+
+def segsort_batch(instances, stream=None) -> None:
+    """Sort every instance of a batch in place with one launch per kernel and key type."""
+    items = batch_items(instances)
+    _check(lib().segsort_pairs_batch(items, len(items), _stream_ptr(stream)), "segsort_pairs_batch")
+
+
+class BatchPlan:
+    """A batch captured once into a CUDA graph; launch() replays it."""
+
+    def __init__(self, instances):
+        self._items = batch_items(instances)
+        self._h = ctypes.c_void_p()
+        _check(lib().segsort_batch_plan_create(self._items, len(self._items), ctypes.byref(self._h)),
+               "segsort_batch_plan_create")
+
+    def launch(self, stream=None) -> None:
+        _check(lib().segsort_batch_plan_launch(self._h, _stream_ptr(stream)), "segsort_batch_plan_launch")
+
+    @property
+    def workspace_bytes(self) -> int:
+        return lib().segsort_batch_plan_workspace_bytes(self._h)
+
+    def close(self) -> None:
+        if self._h:
+            lib().segsort_batch_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,7 +1,8 @@
 """Build recipe of the GB300 segmented sort (in-tree, no cmake).
 
 Products, all written next to this file:
-  libsegsort.so          the C-ABI library (csrc/segsort_api.cu, sm_103a)
+  libsegsort.so          the C-ABI library (csrc/segsort_api.cu: plain calls,
+                         csrc/segsort_batch.cu: batched form; sm_103a)
   segsort_driver.exe     reference-compatible bench driver, prints sorted keys
   segsort_driver_time.exe  the same driver built with ELAPSED_TIME=1
                            EXECUTIONS=10: prints one ms line per execution
@@ -57,9 +58,20 @@ def _run(cmd: list[str], verbose: bool) -> None:
         raise RuntimeError(f"build step failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
+OBJ_DIR = PKG / "_build"
+LIB_UNITS = ["segsort_api.cu", "segsort_batch.cu"]
+
+
+def _obj(unit: str) -> Path:
+    return OBJ_DIR / (Path(unit).stem + ".o")
+
+
+def _obj_cmd(unit: str) -> list[str]:
+    return [nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", "-c", str(CSRC / unit), "-o", str(_obj(unit))]
+
+
 def _lib_cmd() -> list[str]:
-    return [nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", "-shared",
-            str(CSRC / "segsort_api.cu"), "-o", str(LIB)]
+    return [nvcc(), *ARCH, "-shared", *[str(_obj(u)) for u in LIB_UNITS], "-o", str(LIB)]
 
 
 def _driver_cmd(out: Path, timed: bool) -> list[str]:
@@ -82,7 +94,12 @@ def lib_sources() -> list[Path]:
 def build(verbose: bool = False) -> None:
     """Compile the library, the drivers and the generator for sm_103a."""
     lib_in = lib_sources()
-    if _stale(LIB, lib_in):
+    OBJ_DIR.mkdir(exist_ok=True)
+    units = [u for u in LIB_UNITS if _stale(_obj(u), lib_in)]
+    with ThreadPoolExecutor(max_workers=max(1, len(units))) as ex:
+        for f in [ex.submit(_run, _obj_cmd(u), verbose) for u in units]:
+            f.result()
+    if _stale(LIB, [_obj(u) for u in LIB_UNITS]):
         _run(_lib_cmd(), verbose)
     jobs = []
     drv_in = [CSRC / "segsort_driver.cpp", INCLUDE / "segsort.h", LIB]

@@ -130,18 +130,20 @@ __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) {
 //    (off(-1) = -inf, off(nseg) = +inf): the first segment starting in or
 //    after half-tile h, so the tile sort needs no search over the offsets;
 //  * segments longer than cap become jobs of the first level (warp-aggregated
-//    atomic append).
+//    atomic append), tagged with the instance they belong to.
+// Every lane of the warp calls it; `valid` is false for lanes past the end.
 template <typename K>
-__global__ void __launch_bounds__(256)
-large_classify_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
-  const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void classify_boundary(const Offsets &off, int64_t s, bool valid,
+                                                  int64_t cap, int64_t half, int32_t *half_first,
+                                                  int64_t halves, const LargeWs<K> &ws,
+                                                  int32_t inst) {
   const int lane = threadIdx.x & 31;
   int64_t len = 0, cur = 0;
-  if (s <= off.nseg) {
+  if (valid && s <= off.nseg) {
     cur = s < off.nseg ? off(s) : 0;
     const int64_t h_lo = s == 0 ? 0 : off(s - 1) / half + 1;
-    const int64_t h_hi = s == off.nseg ? ws.halves : min(cur / half, ws.halves);
-    for (int64_t h = h_lo; h <= h_hi; ++h) ws.half_first[h] = static_cast<int32_t>(s);
+    const int64_t h_hi = s == off.nseg ? halves : min(cur / half, halves);
+    for (int64_t h = h_lo; h <= h_hi; ++h) half_first[h] = static_cast<int32_t>(s);
     if (s < off.nseg) len = off(s + 1) - cur;
   }
   const bool large = len > cap;
@@ -153,8 +155,67 @@ large_classify_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
   const uint32_t j = base + __popc(ballot & lanemask_lt());
   if (large && j < static_cast<uint32_t>(ws.max_jobs))
     ws.jobs[0][j] = make_int4(static_cast<int32_t>(cur), static_cast<int32_t>(cur + len),
-                              ws.passes, 0);
+                              ws.passes, inst);
 }
+
+template <typename K>
+__global__ void __launch_bounds__(256)
+large_classify_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
+  const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  classify_boundary<K>(off, s, true, cap, half, ws.half_first, ws.halves, ws, 0);
+}
+
+// Batched form: thread g classifies boundary g - bound_base of the instance
+// that owns it; `bounds` is the batch's total of nseg + 1 over its instances.
+template <typename K>
+__global__ void __launch_bounds__(256)
+large_classify_batch_kernel(const BatchInst *__restrict__ tab, int32_t count, int64_t bounds,
+                            int64_t cap, int64_t half, LargeWs<K> ws) {
+  const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool valid = g < bounds;
+  const int32_t i = find_instance(tab, count, valid ? g : 0, &BatchInst::bound_base);
+  const BatchInst &I = tab[i];
+  const int64_t tiles = (I.n + cap - 1) / cap;
+  classify_boundary<K>(I.offsets_view(), g - I.bound_base, valid, cap, half,
+                       ws.half_first + I.half_base, 2 * tiles, ws, i);
+}
+
+// ---------------------------------------------------------------------------
+// Where the long-segment kernel finds an instance's keys and values: the
+// caller's buffers and the instance's region of the temporary buffers, both
+// indexed by instance-local positions.
+template <typename K>
+struct SideBuffers {
+  K *keys;
+  uint32_t *vals;
+  K *tmp_keys;
+  uint32_t *tmp_vals;
+};
+
+// One problem: every job belongs to it.
+template <typename K>
+struct SingleSpace {
+  K *keys;
+  uint32_t *vals;
+  K *tmp_keys;
+  uint32_t *tmp_vals;
+  __device__ __forceinline__ SideBuffers<K> operator()(int32_t) const {
+    return {keys, vals, tmp_keys, tmp_vals};
+  }
+};
+
+// A batch: jobs carry their instance, whose buffers come from the table.
+template <typename K>
+struct BatchSpace {
+  const BatchInst *tab;
+  K *tmp_keys;
+  uint32_t *tmp_vals;
+  __device__ __forceinline__ SideBuffers<K> operator()(int32_t i) const {
+    const BatchInst &I = tab[i];
+    return {static_cast<K *>(I.keys), I.vals, tmp_keys + I.tmp_base,
+            tmp_vals ? tmp_vals + I.tmp_base : nullptr};
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Grid barrier for a cooperative launch (all CTAs resident), bounded.
@@ -220,9 +281,10 @@ struct LargeSmem {
 };
 
 // ---------------------------------------------------------------------------
-template <typename K, bool PAIRS, typename Cfg>
+// Space (SingleSpace or BatchSpace) maps a job's instance to its buffers.
+template <typename K, bool PAIRS, typename Cfg, typename Space>
 __global__ void __launch_bounds__(kLThreads, 1)
-large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> ws) {
+large_sort_kernel(Space sp, LargeWs<K> ws) {
   using Ord = KeyOrder<K>;
   using Bits = typename Ord::Bits;
   constexpr int kItems = PassShape<K>::kItems;
@@ -252,11 +314,8 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
     if (nj == 0) break;
     const int4 *jobs = ws.jobs[cur];
     int4 *next_jobs = ws.jobs[cur ^ 1];
-    // Level parity: even levels scatter keys -> tmp, odd levels tmp -> keys.
-    const K *src_k = cur == 0 ? keys : ws.tmp_keys;
-    K *dst_k = cur == 0 ? ws.tmp_keys : keys;
-    const uint32_t *src_v = cur == 0 ? vals : ws.tmp_vals;
-    uint32_t *dst_v = cur == 0 ? ws.tmp_vals : vals;
+    // Level parity: even levels scatter the caller's buffers into tmp, odd
+    // levels tmp into the caller's buffers.
 
     // ---- P1: chunk prefix (CTA 0); reset per-level counters and arrays --------
     if (blockIdx.x == 0) {
@@ -326,7 +385,10 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         const int4 dsc = ws.desc[t];
         const int64_t cb = dsc.x, e = dsc.y;
         const int32_t j = dsc.z;
-        const int bytes = min(jobs[j].z, passes);
+        const int4 jb = jobs[j];
+        const int bytes = min(jb.z, passes);
+        const SideBuffers<K> B = sp(jb.w);
+        const K *src_k = cur == 0 ? B.keys : B.tmp_keys;
         const int clen = static_cast<int>(min(static_cast<int64_t>(kChunk), e - cb));
         Bits xs[kItems];
 #pragma unroll
@@ -395,12 +457,18 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         }
         const int64_t cb = dsc.x, e = dsc.y, b = dsc.w;
         const int32_t j = dsc.z;
+        const int4 jb = jobs[j];
+        const SideBuffers<K> B = sp(jb.w);
+        const K *src_k = cur == 0 ? B.keys : B.tmp_keys;
+        K *dst_k = cur == 0 ? B.tmp_keys : B.keys;
+        const uint32_t *src_v = cur == 0 ? B.vals : B.tmp_vals;
+        uint32_t *dst_v = cur == 0 ? B.tmp_vals : B.vals;
         const int64_t c = (cb - b) / kChunk;
         const int clen = static_cast<int>(min(static_cast<int64_t>(kChunk), e - cb));
         const uint32_t *jh = ws.hist + static_cast<size_t>(j) * passes * kRadix;
         // Highest byte with two or more non-empty digits.
         int D = kDigitNone;
-        for (int q = min(jobs[j].z, passes) - 1; q >= 0; --q) {
+        for (int q = min(jb.z, passes) - 1; q >= 0; --q) {
           if (__syncthreads_count(tid < kRadix && jh[q * kRadix + tid] != 0) > 1) {
             D = q;
             break;
@@ -535,7 +603,7 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         if (level == 0 && jb.y - jb.x <= CAP) {  // fits the bucket sort: sorted in place
           if (lane == 0) {
             const uint32_t k = atomicAdd(&ws.ctr[kCtrBuckets], 1u);
-            if (k < ws.max_entries) ws.entries[k] = make_int4(jb.x, jb.y - jb.x, 0, kEntryDirect);
+            if (k < ws.max_entries) ws.entries[k] = make_int4(jb.x, jb.y - jb.x, jb.w, kEntryDirect);
           }
           continue;
         }
@@ -559,7 +627,7 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
                 if (walk == 1 && e_base + ne < ws.max_entries)
                   ws.entries[e_base + ne] =
                       make_int4(static_cast<int32_t>(a + o),
-                                static_cast<int32_t>(min(l - o, static_cast<int64_t>(CAP))), 0,
+                                static_cast<int32_t>(min(l - o, static_cast<int64_t>(CAP))), jb.w,
                                 kEntryCopy);
             };
             if (D == kDigitNone) {
@@ -586,7 +654,7 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
                   } else {
                     if (walk == 1 && n_base + nn < static_cast<uint32_t>(ws.max_jobs))
                       next_jobs[n_base + nn] = make_int4(static_cast<int32_t>(jb.x + s0),
-                                                         static_cast<int32_t>(jb.x + s0 + size), D, 0);
+                                                         static_cast<int32_t>(jb.x + s0 + size), D, jb.w);
                     ++nn;
                   }
                   d0 = d + 1;
@@ -645,24 +713,29 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
           if (next_t < nent) next_e = ws.entries[next_t];
         }
         if (en.w == kEntryDirect) {
+          const SideBuffers<K> B = sp(en.z);
           const int64_t a = en.x;
           const int m = en.y;
           if (m > 0 && m <= CAP)
-            sort_chunk<Cfg, PAIRS>(keys + a, PAIRS ? vals + a : nullptr, keys + a,
-                                   PAIRS ? vals + a : nullptr, m, false, [](auto &&) {}, smem,
+            sort_chunk<Cfg, PAIRS>(B.keys + a, PAIRS ? B.vals + a : nullptr, B.keys + a,
+                                   PAIRS ? B.vals + a : nullptr, m, false, [](auto &&) {}, smem,
                                    hb, warp_s);
           continue;
         }
         if (en.w == kEntryCopy) {
+          const SideBuffers<K> B = sp(en.z);
           const int64_t a = en.x;
           const int m = en.y;
           for (int i = tid; i < m; i += kLThreads) {
-            keys[a + i] = ws.tmp_keys[a + i];
-            if constexpr (PAIRS) vals[a + i] = ws.tmp_vals[a + i];
+            B.keys[a + i] = B.tmp_keys[a + i];
+            if constexpr (PAIRS) B.vals[a + i] = B.tmp_vals[a + i];
           }
           continue;
         }
         const int4 jb = jobs[en.x];
+        const SideBuffers<K> B = sp(jb.w);
+        K *dst_k = cur == 0 ? B.tmp_keys : B.keys;
+        uint32_t *dst_v = cur == 0 ? B.tmp_vals : B.vals;
         const int32_t *bs = ws.bstart + static_cast<size_t>(en.x) * (kRadix + 1);
         const int d0 = en.y, d1 = en.z;
         const int64_t s0 = bs[d0];
@@ -672,8 +745,8 @@ large_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, LargeWs<K> 
         // The buckets of one job are ordered by their digit, the highest byte
         // that varies in the job, so sorting the chunk as one segment by the
         // whole key sorts every bucket in it.
-        sort_chunk<Cfg, PAIRS>(dst_k + a, PAIRS ? dst_v + a : nullptr, keys + a,
-                               PAIRS ? vals + a : nullptr, static_cast<int>(m), false,
+        sort_chunk<Cfg, PAIRS>(dst_k + a, PAIRS ? dst_v + a : nullptr, B.keys + a,
+                               PAIRS ? B.vals + a : nullptr, static_cast<int>(m), false,
                                [](auto &&) {},
                                smem, hb, warp_s);
       }

@@ -1,0 +1,366 @@
+// Batched form of the segmented sort: segsort_pairs_batch and batch plans.
+//
+// The instances of a batch are grouped by key type.  A group is sorted by the
+// same three kernels as one plain call -- classify, the cooperative
+// long-segment kernel, the tile sort -- launched once for the whole group:
+// every kernel finds an instance through a device table (BatchInst), tile-sort
+// CTAs and classify threads by binary search over the instances' bases, and
+// long-segment jobs through the instance index they carry.  Small instances
+// therefore share CTAs' worth of work with large ones instead of paying a
+// sequence of launches and grid barriers each.
+//
+// A plan fixes the items, allocates one buffer for every group's table and
+// workspace, and captures the launches into a CUDA graph; a launch replays
+// the graph.
+#include <algorithm>
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "segsort.h"
+#include "segsort_host.cuh"
+
+namespace segsort {
+namespace {
+
+constexpr int kKeyTypes = 4;
+constexpr int64_t kGroupMaxN = (int64_t{1} << 31) - 1;
+
+// Instances of one key type, placed in the batch-wide arrays.
+struct Group {
+  int key_type = 0;
+  std::vector<BatchInst> insts;  // non-empty instances only
+  int64_t total_n = 0, tiles = 0, bounds = 0, half_entries = 0;
+  WsLayout L;
+  size_t tab_off = 0;  // table position in the batch buffer
+  size_t ws_off = 0;   // workspace position in the batch buffer
+};
+
+struct BatchLayout {
+  std::vector<Group> groups;
+  size_t total = 0;
+};
+
+int key_bytes_of(int type) { return type == SEGSORT_KEY_U64 ? 8 : 4; }
+
+int64_t cap_of(int type) {
+  return type == SEGSORT_KEY_U64 ? tile_cap<uint64_t>() : tile_cap<uint32_t>();
+}
+
+int64_t chunk_of(int type) {
+  return type == SEGSORT_KEY_U64 ? PassShape<uint64_t>::kChunk : PassShape<uint32_t>::kChunk;
+}
+
+// Validates the items and lays out every group.  Empty items (n == 0 or
+// nseg == 0) have nothing to sort and are left out.
+int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B) {
+  if (count < 0 || (count > 0 && items == nullptr)) return SEGSORT_ERR_INVALID_ARG;
+  Group g[kKeyTypes];
+  for (int t = 0; t < kKeyTypes; ++t) g[t].key_type = t;
+  for (int32_t i = 0; i < count; ++i) {
+    const segsort_batch_item &it = items[i];
+    if (it.key_type < 0 || it.key_type >= kKeyTypes) return SEGSORT_ERR_INVALID_ARG;
+    if (it.n < 0 || it.nseg < 0 || (it.heads != 0 && it.heads != 1)) return SEGSORT_ERR_INVALID_ARG;
+    if (it.n == 0 || it.nseg == 0) continue;
+    if (it.d_keys == nullptr || it.d_vals == nullptr || it.d_offsets == nullptr)
+      return SEGSORT_ERR_INVALID_ARG;
+    if (it.n >= (int64_t{1} << 30)) return SEGSORT_ERR_TOO_LARGE;
+    Group &G = g[it.key_type];
+    const int64_t cap = cap_of(it.key_type);
+    const int64_t tiles = (it.n + cap - 1) / cap;
+    BatchInst I{};
+    I.keys = it.d_keys;
+    I.vals = it.d_vals;
+    I.offsets = it.d_offsets;
+    I.n = it.n;
+    I.nseg = it.nseg;
+    I.heads = it.heads;
+    I.tmp_base = G.total_n;
+    I.half_base = G.half_entries;
+    I.tile_base = G.tiles;
+    I.bound_base = G.bounds;
+    G.insts.push_back(I);
+    G.total_n += it.n;
+    G.half_entries += 2 * tiles + 1;
+    G.tiles += tiles;
+    G.bounds += static_cast<int64_t>(it.nseg) + 1;
+    if (G.total_n > kGroupMaxN) return SEGSORT_ERR_TOO_LARGE;
+  }
+  size_t off = 0;
+  for (int t = 0; t < kKeyTypes; ++t) {
+    Group &G = g[t];
+    if (G.insts.empty()) continue;
+    G.L = make_layout(G.total_n, key_bytes_of(t), 4, cap_of(t), chunk_of(t), G.half_entries);
+    G.tab_off = off;
+    off = align256(off + G.insts.size() * sizeof(BatchInst));
+    G.ws_off = off;
+    off = align256(off + G.L.total);
+    B.groups.push_back(std::move(G));
+  }
+  B.total = off;
+  return SEGSORT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Table upload without host synchronisation: the entries travel as kernel
+// parameters (one launch per block of kUploadBlock entries), so the host
+// array may be freed as soon as the launch returns.
+constexpr int kUploadBlock = 48;  // 48 * 72 bytes: inside the 4 KB parameter space
+struct UploadBlock {
+  BatchInst v[kUploadBlock];
+  int32_t count;
+};
+static_assert(sizeof(UploadBlock) <= 4096, "kernel parameters must fit 4 KB");
+
+__global__ void upload_insts_kernel(UploadBlock blk, BatchInst *dst) {
+  if (static_cast<int32_t>(threadIdx.x) < blk.count) dst[threadIdx.x] = blk.v[threadIdx.x];
+}
+
+cudaError_t upload_table(const std::vector<BatchInst> &v, BatchInst *dst, cudaStream_t stream) {
+  for (size_t i = 0; i < v.size(); i += kUploadBlock) {
+    UploadBlock blk;
+    std::memset(&blk, 0, sizeof(blk));
+    blk.count = static_cast<int32_t>(std::min<size_t>(kUploadBlock, v.size() - i));
+    std::copy(v.begin() + i, v.begin() + i + blk.count, blk.v);
+    upload_insts_kernel<<<1, kUploadBlock, 0, stream>>>(blk, dst + i);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels of one key type, their one-time attributes and launch shapes.
+template <typename K>
+struct BatchKernels {
+  using TCfg = typename TileFor<K, true>::Cfg;
+  using LCfg = typename LargeFor<K, true>::Cfg;
+  using LS = LargeSmem<K, true, LCfg>;
+  static constexpr auto tile = tile_sort_batch_kernel<K, true, TCfg::NT, TCfg::KPT,
+                                                      TileFor<K, true>::kMinBlocks>;
+  static constexpr auto large = large_sort_kernel<K, true, LCfg, BatchSpace<K>>;
+  static constexpr auto classify = large_classify_batch_kernel<K>;
+  static inline std::atomic<uint64_t> tile_attr{0}, large_attr{0};
+  static inline std::atomic<int> large_occ[kMaxDevices];
+
+  // Attributes and occupancy, before any capture.
+  static cudaError_t prepare(int dev) {
+    cudaError_t e = ensure_smem(tile, TCfg::kSmemBytes, tile_attr, dev);
+    if (e == cudaSuccess) e = ensure_smem(large, LS::kBytes, large_attr, dev);
+    if (e == cudaSuccess) occupancy(large, kLThreads, LS::kBytes, large_occ, dev);
+    return e;
+  }
+
+  static int enqueue(const Group &G, unsigned char *buf, const DeviceState &S, int dev,
+                     cudaStream_t stream) {
+    const BatchInst *tab = reinterpret_cast<const BatchInst *>(buf + G.tab_off);
+    const int32_t count = static_cast<int32_t>(G.insts.size());
+    const LargeWs<K> W = ws_views<K, true>(buf + G.ws_off, G.L);
+    const int64_t cap = tile_cap<K>();
+    if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess)
+      return SEGSORT_ERR_CUDA;
+    const unsigned cls_blocks = static_cast<unsigned>((G.bounds + 255) / 256);
+    classify<<<cls_blocks, 256, 0, stream>>>(tab, count, G.bounds, cap, cap / 2, W);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+
+    const int lo = occupancy(large, kLThreads, LS::kBytes, large_occ, dev);
+    const int64_t chunks = (G.total_n + PassShape<K>::kChunk - 1) / PassShape<K>::kChunk;
+    const unsigned grid =
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S.sms, chunks));
+    BatchSpace<K> sp{tab, W.tmp_keys, W.tmp_vals};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kLThreads);
+    cfg.dynamicSmemBytes = LS::kBytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, large, sp, W) != cudaSuccess) return SEGSORT_ERR_CUDA;
+
+    tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, TCfg::kSmemBytes, stream>>>(tab, count,
+                                                                                W.half_first);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    return SEGSORT_OK;
+  }
+};
+
+cudaError_t prepare_group(const Group &G, int dev) {
+  switch (G.key_type) {
+    case SEGSORT_KEY_U32: return BatchKernels<uint32_t>::prepare(dev);
+    case SEGSORT_KEY_I32: return BatchKernels<int32_t>::prepare(dev);
+    case SEGSORT_KEY_F32: return BatchKernels<float>::prepare(dev);
+    default: return BatchKernels<uint64_t>::prepare(dev);
+  }
+}
+
+int enqueue_group(const Group &G, unsigned char *buf, const DeviceState &S, int dev,
+                  cudaStream_t stream) {
+  switch (G.key_type) {
+    case SEGSORT_KEY_U32: return BatchKernels<uint32_t>::enqueue(G, buf, S, dev, stream);
+    case SEGSORT_KEY_I32: return BatchKernels<int32_t>::enqueue(G, buf, S, dev, stream);
+    case SEGSORT_KEY_F32: return BatchKernels<float>::enqueue(G, buf, S, dev, stream);
+    default: return BatchKernels<uint64_t>::enqueue(G, buf, S, dev, stream);
+  }
+}
+
+int prepare_all(const BatchLayout &B, int dev) {
+  for (const Group &G : B.groups)
+    if (prepare_group(G, dev) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  return SEGSORT_OK;
+}
+
+int enqueue_all(const BatchLayout &B, unsigned char *buf, const DeviceState &S, int dev,
+                cudaStream_t stream) {
+  for (const Group &G : B.groups) {
+    const int rc = enqueue_group(G, buf, S, dev, stream);
+    if (rc != SEGSORT_OK) return rc;
+  }
+  return SEGSORT_OK;
+}
+
+int current_device(int *dev, DeviceState **S) {
+  if (cudaGetDevice(dev) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  *S = device_state(*dev);
+  if (*S == nullptr || !(*S)->coop) return SEGSORT_ERR_CUDA;
+  return SEGSORT_OK;
+}
+
+}  // namespace
+
+cudaError_t batch_device_status(bool clear, uint32_t *value) {
+  cudaError_t e = cudaMemcpyFromSymbol(value, g_device_status, sizeof(uint32_t));
+  if (e == cudaSuccess && clear) {
+    const uint32_t zero = 0;
+    e = cudaMemcpyToSymbol(g_device_status, &zero, sizeof(zero));
+  }
+  return e;
+}
+
+}  // namespace segsort
+
+struct segsort_batch_plan_s {
+  int dev = 0;
+  void *buf = nullptr;
+  size_t bytes = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int segsort_pairs_batch(const segsort_batch_item *items, int32_t count, segsort_stream_t s) {
+  using namespace segsort;
+  const cudaStream_t stream = reinterpret_cast<cudaStream_t>(s);
+  BatchLayout B;
+  int rc = build_layout(items, count, B);
+  if (rc != SEGSORT_OK || B.groups.empty()) return rc;
+  int dev = 0;
+  DeviceState *S = nullptr;
+  if ((rc = current_device(&dev, &S)) != SEGSORT_OK) return rc;
+  if ((rc = prepare_all(B, dev)) != SEGSORT_OK) return rc;
+  cudaMemPool_t pool = device_pool(*S, dev);
+  unsigned char *buf = nullptr;
+  if (pool == nullptr ||
+      cudaMallocFromPoolAsync(reinterpret_cast<void **>(&buf), B.total, pool, stream) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return SEGSORT_ERR_NO_MEMORY;
+  }
+  for (const Group &G : B.groups) {
+    if (upload_table(G.insts, reinterpret_cast<BatchInst *>(buf + G.tab_off), stream) !=
+        cudaSuccess) {
+      rc = SEGSORT_ERR_CUDA;
+      break;
+    }
+  }
+  if (rc == SEGSORT_OK) rc = enqueue_all(B, buf, *S, dev, stream);
+  if (cudaFreeAsync(buf, stream) != cudaSuccess && rc == SEGSORT_OK) rc = SEGSORT_ERR_CUDA;
+  return rc;
+}
+
+int segsort_batch_plan_create(const segsort_batch_item *items, int32_t count,
+                              segsort_batch_plan *plan) {
+  using namespace segsort;
+  if (plan == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  *plan = nullptr;
+  BatchLayout B;
+  int rc = build_layout(items, count, B);
+  if (rc != SEGSORT_OK) return rc;
+  int dev = 0;
+  DeviceState *S = nullptr;
+  if ((rc = current_device(&dev, &S)) != SEGSORT_OK) return rc;
+  if ((rc = prepare_all(B, dev)) != SEGSORT_OK) return rc;
+
+  segsort_batch_plan_s *P = new (std::nothrow) segsort_batch_plan_s;
+  if (P == nullptr) return SEGSORT_ERR_NO_MEMORY;
+  P->dev = dev;
+  P->bytes = B.total;
+  cudaStream_t cs = nullptr;
+  do {
+    if (B.total > 0 && cudaMalloc(&P->buf, B.total) != cudaSuccess) {
+      cudaGetLastError();
+      rc = SEGSORT_ERR_NO_MEMORY;
+      break;
+    }
+    unsigned char *buf = static_cast<unsigned char *>(P->buf);
+    for (const Group &G : B.groups) {
+      if (cudaMemcpy(buf + G.tab_off, G.insts.data(), G.insts.size() * sizeof(BatchInst),
+                     cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+    }
+    if (rc != SEGSORT_OK) break;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      rc = SEGSORT_ERR_CUDA;
+      break;
+    }
+    rc = enqueue_all(B, buf, *S, dev, cs);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+    if (rc == SEGSORT_OK && ce != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+    P->graph = graph;
+    if (rc != SEGSORT_OK) break;
+    if (cudaGraphInstantiate(&P->exec, P->graph, 0) != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+  } while (false);
+  if (cs != nullptr) cudaStreamDestroy(cs);
+  if (rc != SEGSORT_OK) {
+    cudaGetLastError();
+    segsort_batch_plan_destroy(P);
+    return rc;
+  }
+  *plan = P;
+  return SEGSORT_OK;
+}
+
+int segsort_batch_plan_launch(segsort_batch_plan plan, segsort_stream_t s) {
+  if (plan == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  if (plan->exec == nullptr) return SEGSORT_OK;  // nothing to sort
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != plan->dev) return SEGSORT_ERR_INVALID_ARG;
+  return cudaGraphLaunch(plan->exec, reinterpret_cast<cudaStream_t>(s)) == cudaSuccess
+             ? SEGSORT_OK
+             : SEGSORT_ERR_CUDA;
+}
+
+size_t segsort_batch_plan_workspace_bytes(segsort_batch_plan plan) {
+  return plan == nullptr ? 0 : plan->bytes;
+}
+
+void segsort_batch_plan_destroy(segsort_batch_plan plan) {
+  if (plan == nullptr) return;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  if (plan->buf) cudaFree(plan->buf);
+  delete plan;
+}
+
+}  // extern "C"

@@ -73,6 +73,41 @@ struct Offsets {
 };
 
 // ---------------------------------------------------------------------------
+// One instance of a batched call, as the kernels see it.  A batch is a list of
+// independent (keys, values, offsets) problems of one key type sorted by one
+// launch of each kernel.  Every per-instance index is instance-local; the
+// *_base fields place the instance in the batch-wide arrays: its region of
+// the temporary key/value buffers, its half-tile map, its tile-sort CTAs and
+// its classify threads (one per segment boundary, nseg + 1 of them).
+// ---------------------------------------------------------------------------
+struct BatchInst {
+  void *keys;
+  uint32_t *vals;
+  const int32_t *offsets;
+  int64_t n;
+  int64_t tmp_base;
+  int64_t half_base;
+  int64_t tile_base;
+  int64_t bound_base;
+  int32_t nseg;
+  int32_t heads;
+
+  __device__ __forceinline__ Offsets offsets_view() const { return Offsets{offsets, nseg, heads, n}; }
+};
+
+// The last instance whose `field` is at or below x (instances with equal
+// bases own nothing before the next one; the host drops empty instances).
+__device__ __forceinline__ int32_t find_instance(const BatchInst *tab, int32_t count, int64_t x,
+                                                 int64_t BatchInst::*field) {
+  int32_t lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int32_t mid = (lo + hi + 1) >> 1;
+    if (tab[mid].*field <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
 // Device status word: kernels OR error bits into it; the host reads it back
 // with segsort_device_status().
 // ---------------------------------------------------------------------------
@@ -80,9 +115,9 @@ enum : uint32_t {
   kStatusTimeout = 1u,
 };
 
-// Defined here: the library is one translation unit (segsort_api.cu), which
-// is the only file that includes this header.
-__device__ uint32_t g_device_status = 0;
+// One word per translation unit of the library (internal linkage); the host
+// reads every unit's word.
+static __device__ uint32_t g_device_status = 0;
 
 __device__ __forceinline__ void raise_status(uint32_t bits) {
   atomicOr(&g_device_status, bits);

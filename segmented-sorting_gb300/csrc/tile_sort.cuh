@@ -689,13 +689,14 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
 }
 
 // ---------------------------------------------------------------------------
-// The kernel.  With half_first == null the problem is one tile (n <= CAP):
-// one chunk with every segment.
+// One CTA of the tile sort: tile t of a problem whose half-tile map is
+// half_first (null: the problem is one tile, n <= CAP, and the CTA sorts one
+// chunk with every segment).
 // ---------------------------------------------------------------------------
-template <typename K, bool PAIRS, int NT, int KPT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
-                 const int32_t *__restrict__ half_first) {
+template <typename K, bool PAIRS, int NT, int KPT>
+__device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restrict__ vals,
+                                         const Offsets &off, const int32_t *__restrict__ half_first,
+                                         int64_t t) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   constexpr int CAP = Cfg::CAP;
   constexpr int64_t HALF = Cfg::HALF;
@@ -710,7 +711,6 @@ tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
   const int tid = threadIdx.x;
   const int64_t n = off.n;
   const int64_t nseg = off.nseg;
-  const int64_t t = blockIdx.x;
   if (t * CAP >= n) return;
 
   if (tid == 0) {
@@ -761,6 +761,33 @@ tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                            },
                            smem, hb, warp_s);
   }
+}
+
+// ---------------------------------------------------------------------------
+// The kernel: CTA t sorts tile t.
+// ---------------------------------------------------------------------------
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
+                 const int32_t *__restrict__ half_first) {
+  tile_cta<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: the tiles of every instance of a batch in one launch.  CTA t
+// belongs to the last instance whose first tile is at or before t and sorts
+// that instance's local tile; each instance has its own half-tile map, so a
+// CTA never mixes instances.
+// ---------------------------------------------------------------------------
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_sort_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
+                       const int32_t *__restrict__ half_first) {
+  const int64_t t = blockIdx.x;
+  const int32_t i = find_instance(tab, count, t, &BatchInst::tile_base);
+  const BatchInst &I = tab[i];
+  tile_cta<K, PAIRS, NT, KPT>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
+                              half_first + I.half_base, t - I.tile_base);
 }
 
 }  // namespace segsort

@@ -111,6 +111,65 @@ def lognormal_offsets(n: int, seed: int = 1, mu: float = 4.0, sigma: float = 2.5
     return off.astype(np.int32)
 
 
+def equal_offsets_ragged(n: int, length: int) -> np.ndarray:
+    """n // length equal segments and, when length does not divide n, one
+    shorter last segment, so every element is in a segment."""
+    off = equal_offsets(n, length).astype(np.int64)
+    if off[-1] < n:
+        off = np.concatenate([off, [n]])
+    return off.astype(np.int32)
+
+
+def typed_keys(n: int, seed: int, key_type: str) -> np.ndarray:
+    """Keys of a batch instance: u32 / i32 / u64 uniform over the type's
+    range, f32 uniform in [-1000, 1000) (both signs, no NaN)."""
+    if key_type == "u32":
+        return uniform_keys(n, seed, 32)
+    if key_type == "i32":
+        return uniform_keys(n, seed, 32).view(np.int32)
+    if key_type == "u64":
+        return uniform_keys(n, seed, 64, np.uint64)
+    if key_type == "f32":
+        return ((_unit(draw(seed, 0, 0, n)) * 2.0 - 1.0) * 1000.0).astype(np.float32)
+    raise ValueError(key_type)
+
+
+BATCH_KEY_TYPES = ("u32", "u64", "f32")
+
+
+def batch_specs(count: int = 64, seed: int = 4, lo_log: float = 16, hi_log: float = 24,
+                key_types=BATCH_KEY_TYPES) -> list[dict]:
+    """Shapes of the mixed batch: n log-uniform in [2^lo_log, 2^hi_log];
+    segment lengths equal (length log-uniform in [2, 2^16], ragged last
+    segment) or lognormal as in the uneven workload, each with probability
+    1/2; key types cycle through key_types."""
+    u = _unit(draw(seed, 6, 0, 3 * count))
+    specs = []
+    for i in range(count):
+        n = int(round(2.0 ** (lo_log + (hi_log - lo_log) * u[3 * i])))
+        specs.append({
+            "n": n,
+            "dist": "equal" if u[3 * i + 1] < 0.5 else "lognormal",
+            "length": int(round(2.0 ** (1 + 15 * u[3 * i + 2]))),
+            "key_type": key_types[i % len(key_types)],
+            "seed": seed * 1000 + i,
+        })
+    return specs
+
+
+def batch_offsets(spec: dict) -> np.ndarray:
+    """Offsets of one batch instance."""
+    n = spec["n"]
+    if spec["dist"] == "equal":
+        return equal_offsets_ragged(n, spec["length"])
+    return lognormal_offsets(n, spec["seed"])
+
+
+def batch_instance(spec: dict):
+    """(offsets, keys) of one batch instance."""
+    return batch_offsets(spec), typed_keys(spec["n"], spec["seed"], spec["key_type"])
+
+
 def instance(workload: str, n: int, seed: int = 1, length: int = 0, nseg: int = 0,
              bits: int = 32):
     """(offsets, keys) of a named workload."""
@@ -137,14 +196,34 @@ def _srl(t, k: int):
     return (t >> k) & ((1 << (64 - k)) - 1)
 
 
-def device_uniform_keys(n: int, seed: int = 1, bits: int = 32, device="cuda"):
-    """int32 CUDA tensor holding the uint32 bits of uniform_keys(n, seed, bits)."""
+def device_draw(n: int, seed: int, lane: int = 0, device="cuda"):
+    """int64 CUDA tensor holding the bits of draw(seed, lane, 0, n)."""
     import torch
-    base = _s64(seed * 0x9E3779B97F4A7C15 + 1)
+    base = _s64(seed * 0x9E3779B97F4A7C15 + lane * 0xD1B54A32D192ED03 + 1)
     x = torch.arange(n, dtype=torch.int64, device=device) + base
     x = x + _s64(0x9E3779B97F4A7C15)
     x = (x ^ _srl(x, 30)) * _s64(0xBF58476D1CE4E5B9)
     x = (x ^ _srl(x, 27)) * _s64(0x94D049BB133111EB)
-    x = x ^ _srl(x, 31)
-    k = _srl(x, 64 - bits)
+    return x ^ _srl(x, 31)
+
+
+def device_uniform_keys(n: int, seed: int = 1, bits: int = 32, device="cuda"):
+    """int32 CUDA tensor holding the uint32 bits of uniform_keys(n, seed, bits)."""
+    import torch
+    k = _srl(device_draw(n, seed, 0, device), 64 - bits)
     return (k - (k >= (1 << 31)).to(torch.int64) * (1 << 32)).to(torch.int32)
+
+
+def device_typed_keys(n: int, seed: int, key_type: str, device="cuda"):
+    """CUDA tensor with the bits of typed_keys(n, seed, key_type): int32 for
+    u32/i32, float32 for f32, int64 for u64."""
+    import torch
+    if key_type in ("u32", "i32"):
+        return device_uniform_keys(n, seed, 32, device)
+    x = device_draw(n, seed, 0, device)
+    if key_type == "u64":
+        return x
+    if key_type == "f32":
+        u = (_srl(x, 11).to(torch.float64) + 0.5) * (1.0 / 9007199254740992.0)
+        return ((u * 2.0 - 1.0) * 1000.0).to(torch.float32)
+    raise ValueError(key_type)

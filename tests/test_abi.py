@@ -88,3 +88,43 @@ def test_error_strings_and_version(pkg):
     for code in range(0, -7, -1):
         assert L.segsort_error_string(code)
     assert L.segsort_version() >= 100
+
+
+def test_batch_host_side_argument_checks(pkg):
+    """The batched entry points validate every item before any CUDA call."""
+    L = pkg.lib()
+    P = ctypes.c_void_p(16)
+
+    def items(*specs):
+        return (pkg.BatchItem * len(specs))(*[pkg.BatchItem(*s) for s in specs])
+
+    ok = (0, 0, 16, 16, 100, 16, 1, 0)
+    # nothing to sort: empty list, or only empty items
+    assert L.segsort_pairs_batch(None, 0, None) == pkg.SEGSORT_OK
+    assert L.segsort_pairs_batch(items((0, 0, None, None, 0, None, 0, 0)), 1, None) == pkg.SEGSORT_OK
+    assert L.segsort_pairs_batch(None, 3, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_pairs_batch(items(ok), -1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    bad = [
+        (7, 0, 16, 16, 100, 16, 1, 0),      # unknown key type
+        (0, 2, 16, 16, 100, 16, 1, 0),      # heads flag not 0/1
+        (0, 0, 16, 16, -1, 16, 1, 0),       # n < 0
+        (0, 0, 16, 16, 100, 16, -1, 0),     # nseg < 0
+        (0, 0, None, 16, 100, 16, 1, 0),    # null keys
+        (2, 0, 16, None, 100, 16, 1, 0),    # null values
+        (3, 0, 16, 16, 100, None, 1, 0),    # null offsets
+    ]
+    for b in bad:
+        assert L.segsort_pairs_batch(items(ok, b), 2, None) == pkg.SEGSORT_ERR_INVALID_ARG, b
+    assert L.segsort_pairs_batch(items((0, 0, 16, 16, 1 << 30, 16, 1, 0)), 1,
+                                 None) == pkg.SEGSORT_ERR_TOO_LARGE
+    # one key type's items together at most 2^31 - 1 elements
+    big = (1, 0, 16, 16, (1 << 30) - 1, 16, 1, 0)
+    assert L.segsort_pairs_batch(items(big, big, big), 3, None) == pkg.SEGSORT_ERR_TOO_LARGE
+    plan = ctypes.c_void_p()
+    assert L.segsort_batch_plan_create(items(bad[0]), 1, ctypes.byref(plan)) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert not plan.value
+    assert L.segsort_batch_plan_create(items(ok), 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_batch_plan_launch(None, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_batch_plan_workspace_bytes(None) == 0
+    L.segsort_batch_plan_destroy(None)
+    del P
