@@ -65,6 +65,9 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the 64-instance batch")
     p.add_argument("--no-configs", action="store_true", help="skip the other workloads")
+    p.add_argument("--no-served", action="store_true", help="skip the served-form stream")
+    p.add_argument("--served-requests", type=int, default=1000)
+    p.add_argument("--served-rates", type=str, default="1000,10000,50000")
     return p.parse_args()
 
 
@@ -318,6 +321,26 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
     }
 
 
+SERVED_WORKLOAD = ("Poisson request stream, seed 7; each request a uint32 key/value sort with "
+                   "n log-uniform in [2^10, 2^24] and lognormal(4, 2.5) segment lengths (1% empty); "
+                   "64 GB HBM admission budget; inputs and outputs in pinned host memory")
+
+
+def bench_served(requests: int, rates: str) -> dict:
+    """The served form against the one-request-per-call loop, through the
+    native driver serve_bench.exe (one JSON line per arrival rate)."""
+    exe = entry.PKG_DIR / "serve_bench.exe"
+    cmd = [str(exe), "--requests", str(requests), "--rates", rates, "--budget-gb", "64",
+           "--seed", "7"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=1200)
+    if r.returncode != 0:
+        raise RuntimeError(f"serve_bench failed ({r.returncode}): {r.stderr[-2000:]}")
+    rows = [json.loads(line) for line in r.stdout.splitlines() if line.strip()]
+    return {"workload": SERVED_WORKLOAD,
+            "sample": f"{requests} requests per rate (the same requests at every rate)",
+            "rates": rows}
+
+
 def bench_configs(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
     """The plain call on the other single-instance workloads: 2^20 keys-only
     (1024 x 1024, keys < 2^31) and 2^25 pairs with lognormal segment lengths
@@ -473,7 +496,7 @@ def run_ours(args) -> None:
         ms_sum = sum(phase[lg]["tile_ms"] for lg in lens_in)
         launches = len(lens_in)
     else:
-        name = "large-segment radix passes (hist + 4 scatter passes)"
+        name = "large_sort_kernel"
         lens_in = [lg for lg in lengths if (1 << lg) > cap]
         ms_sum = sum(phase[lg]["large_ms"] for lg in lens_in)
         launches = len(lens_in)
@@ -484,7 +507,7 @@ def run_ours(args) -> None:
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_kind": f"{peak_kind} hbm_gbs (copy)",
                 "algorithmic_bytes_per_launch": alg_bytes // max(launches, 1),
-                "traffic": (tr or {}).get(name.split()[0]) if tr else None,
+                "traffic": (tr or {}).get(name) if tr else None,
                 "phase_ms_per_step": {"tile": round(tile_ms, 4), "large": round(large_ms, 4)}}
 
     # ---- end to end through the public API with host buffers ---------------
@@ -542,6 +565,9 @@ def run_ours(args) -> None:
     # ---- the batched form and the other workloads ---------------------------
     batched = None if args.no_batched else bench_batched(pkg, inst, dev, stream, 2, 5)
     configs = None if args.no_configs else bench_configs(pkg, inst, dev, stream, 3, 10)
+    served = None
+    if rank == 0 and not args.no_served:
+        served = bench_served(args.served_requests, args.served_rates)
 
     # ---- CPU baseline (rank 0) ----------------------------------------------
     cpu = None
@@ -568,7 +594,7 @@ def run_ours(args) -> None:
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(), "per_len": per_len,
-            "batched": batched, "configs": configs,
+            "batched": batched, "configs": configs, "served": served,
         }), flush=True)
     if world > 1:
         dist.destroy_process_group()

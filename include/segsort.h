@@ -208,6 +208,62 @@ int segsort_batch_plan_launch(segsort_batch_plan plan, segsort_stream_t stream);
 size_t segsort_batch_plan_workspace_bytes(segsort_batch_plan plan);
 void segsort_batch_plan_destroy(segsort_batch_plan plan);
 
+/* Device bytes one segsort_pairs_batch call on these items takes from the
+ * library's pool (tables and workspace); 0 when the items are invalid or
+ * hold nothing to sort. */
+size_t segsort_batch_workspace_bytes(const segsort_batch_item *items, int32_t count);
+
+/* ------------------------------------------------------------------------
+ * Served form: a continuous-batching request server on the current device.
+ * No counterpart in the reference (its programs sort one instance read from
+ * stdin, src/mseq.cu:57-67).
+ *
+ * Requests are uint32 key/value sorts whose inputs and outputs live in host
+ * memory (pin it, e.g. cudaHostAlloc, for copies that overlap the sorts).
+ * submit() only queues the request and returns a ticket.  A worker thread
+ * admits queued requests in arrival order while their device footprint
+ * (keys, values, offsets and sort workspace) fits the HBM budget next to the
+ * requests already in flight, coalesces every admitted request into one
+ * batched sort (segsort_pairs_batch), and keeps up to `depth` batches in the
+ * pipeline: the copies in of the next batch and the copies out of the last
+ * one overlap the current sort.  Requests that arrive while a batch runs join
+ * the next one.  A request whose footprint alone exceeds the budget is refused
+ * (SEGSORT_ERR_TOO_LARGE).  The result of every request is bit for bit the
+ * result of its own plain call.
+ * ---------------------------------------------------------------------- */
+typedef struct segsort_server_s *segsort_server;
+typedef struct segsort_server_stats {
+  int64_t requests;         /* completed requests                         */
+  int64_t batches;          /* batched sorts launched                     */
+  int64_t keys;             /* keys of the completed requests             */
+  int64_t max_batch;        /* most requests coalesced into one batch     */
+  int64_t peak_bytes;       /* highest admitted device footprint          */
+  int64_t budget_waits;     /* admissions that left the oldest queued
+                               request waiting for memory to be released  */
+  int32_t status;           /* first error of the worker, SEGSORT_OK      */
+  int32_t reserved;
+} segsort_server_stats;
+
+/* budget_bytes: device bytes the in-flight requests may hold;
+ * max_batch_keys: a batch closes once it holds this many keys (0: 2^26;
+ * a single larger request still forms a batch of its own); max_batch: most
+ * requests per batch (0: no limit); depth: batches in the pipeline (1..8,
+ * 0: 2). */
+int segsort_server_create(size_t budget_bytes, int64_t max_batch_keys, int32_t max_batch,
+                          int32_t depth, segsort_server *server);
+int segsort_server_submit(segsort_server server, const uint32_t *h_keys,
+                          const uint32_t *h_vals, int64_t n, const int32_t *h_offsets,
+                          int32_t nseg, uint32_t *h_keys_out, uint32_t *h_vals_out,
+                          uint64_t *ticket);
+/* Blocks until the request is done; *latency_ms (optional) = completion
+ * minus submission, host steady clock. */
+int segsort_server_wait(segsort_server server, uint64_t ticket, double *latency_ms);
+/* Blocks until every submitted request is done. */
+int segsort_server_drain(segsort_server server);
+int segsort_server_get_stats(segsort_server server, segsort_server_stats *stats);
+/* Drains, stops the worker and frees the server. */
+void segsort_server_destroy(segsort_server server);
+
 /* ------------------------------------------------------------------------
  * Diagnostics.
  * segsort_device_status() synchronises the current device, returns

@@ -41,6 +41,14 @@ class BatchItem(ctypes.Structure):
                 ("n", ctypes.c_int64), ("d_offsets", ctypes.c_void_p),
                 ("nseg", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
+class ServerStats(ctypes.Structure):
+    """segsort_server_stats of include/segsort.h."""
+    _fields_ = [("requests", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("keys", ctypes.c_int64), ("max_batch", ctypes.c_int64),
+                ("peak_bytes", ctypes.c_int64), ("budget_waits", ctypes.c_int64),
+                ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 # Every symbol include/segsort.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -59,6 +67,14 @@ SIGNATURES = {
     "segsort_batch_plan_launch": ([_P, _P], ctypes.c_int),
     "segsort_batch_plan_workspace_bytes": ([_P], ctypes.c_size_t),
     "segsort_batch_plan_destroy": ([_P], None),
+    "segsort_batch_workspace_bytes": ([ctypes.POINTER(BatchItem), _I32], ctypes.c_size_t),
+    "segsort_server_create": ([ctypes.c_size_t, _I64, _I32, _I32, ctypes.POINTER(_P)], ctypes.c_int),
+    "segsort_server_submit": ([_P, _P, _P, _I64, _P, _I32, _P, _P, ctypes.POINTER(ctypes.c_uint64)],
+                              ctypes.c_int),
+    "segsort_server_wait": ([_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "segsort_server_drain": ([_P], ctypes.c_int),
+    "segsort_server_get_stats": ([_P, ctypes.POINTER(ServerStats)], ctypes.c_int),
+    "segsort_server_destroy": ([_P], None),
     "segsort_device_status": ([ctypes.c_int], ctypes.c_int),
     "segsort_error_string": ([ctypes.c_int], ctypes.c_char_p),
     "segsort_version": ([], ctypes.c_int),
@@ -242,6 +258,65 @@ class BatchPlan:
         if self._h:
             lib().segsort_batch_plan_destroy(self._h)
             self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# Served form.
+# ---------------------------------------------------------------------------
+class Server:
+    """Continuous-batching request server on the current device.
+
+    submit() takes host buffers (numpy arrays or CPU tensors; pinned memory
+    lets the copies overlap the sorts) that must stay alive until wait()
+    returns for that ticket; results land in keys_out / vals_out."""
+
+    def __init__(self, budget_bytes: int, max_batch: int = 0, depth: int = 0,
+                 max_batch_keys: int = 0):
+        self._h = ctypes.c_void_p()
+        _check(lib().segsort_server_create(budget_bytes, max_batch_keys, max_batch, depth,
+                                           ctypes.byref(self._h)), "segsort_server_create")
+        self._keep = {}
+
+    @staticmethod
+    def _ptr(a) -> int:
+        return a.ctypes.data if hasattr(a, "ctypes") else a.data_ptr()
+
+    def submit(self, keys, vals, offsets, keys_out, vals_out) -> int:
+        t = ctypes.c_uint64()
+        n = len(keys)
+        _check(lib().segsort_server_submit(self._h, self._ptr(keys), self._ptr(vals), n,
+                                           self._ptr(offsets), len(offsets) - 1,
+                                           self._ptr(keys_out), self._ptr(vals_out),
+                                           ctypes.byref(t)), "segsort_server_submit")
+        self._keep[t.value] = (keys, vals, offsets, keys_out, vals_out)
+        return t.value
+
+    def wait(self, ticket: int) -> float:
+        ms = ctypes.c_double()
+        rc = lib().segsort_server_wait(self._h, ticket, ctypes.byref(ms))
+        self._keep.pop(ticket, None)
+        _check(rc, "segsort_server_wait")
+        return ms.value
+
+    def drain(self) -> None:
+        _check(lib().segsort_server_drain(self._h), "segsort_server_drain")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().segsort_server_get_stats(self._h, ctypes.byref(st)), "segsort_server_get_stats")
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_ if f != "reserved"}
+
+    def close(self) -> None:
+        if self._h:
+            lib().segsort_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._keep.clear()
 
     def __del__(self):
         try:

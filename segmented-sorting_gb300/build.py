@@ -2,7 +2,9 @@
 
 Products, all written next to this file:
   libsegsort.so          the C-ABI library (csrc/segsort_api.cu: plain calls,
-                         csrc/segsort_batch.cu: batched form; sm_103a)
+                         csrc/segsort_batch.cu: batched form,
+                         csrc/segsort_server.cu: served form; sm_103a)
+  serve_bench.exe        served-form benchmark driver (Poisson request stream)
   segsort_driver.exe     reference-compatible bench driver, prints sorted keys
   segsort_driver_time.exe  the same driver built with ELAPSED_TIME=1
                            EXECUTIONS=10: prints one ms line per execution
@@ -32,6 +34,7 @@ LIB = PKG / "libsegsort.so"
 DRIVER = PKG / "segsort_driver.exe"
 DRIVER_TIME = PKG / "segsort_driver_time.exe"
 GEN = PKG / "gen_instance.exe"
+SERVE = PKG / "serve_bench.exe"
 
 
 def nvcc() -> str:
@@ -59,7 +62,7 @@ def _run(cmd: list[str], verbose: bool) -> None:
 
 
 OBJ_DIR = PKG / "_build"
-LIB_UNITS = ["segsort_api.cu", "segsort_batch.cu"]
+LIB_UNITS = ["segsort_api.cu", "segsort_batch.cu", "segsort_server.cu"]
 
 
 def _obj(unit: str) -> Path:
@@ -83,6 +86,13 @@ def _driver_cmd(out: Path, timed: bool) -> list[str]:
             f"-Wl,-rpath,{cuda / 'lib64'}"]
 
 
+def _serve_cmd() -> list[str]:
+    cuda = cuda_home()
+    return ["g++", "-O2", "-std=c++17", "-pthread", f"-I{INCLUDE}", f"-I{cuda / 'include'}",
+            str(CSRC / "serve_bench.cpp"), "-o", str(SERVE), f"-L{PKG}", "-lsegsort",
+            f"-L{cuda / 'lib64'}", "-lcudart", "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath,{cuda / 'lib64'}"]
+
+
 def _gen_cmd() -> list[str]:
     return ["g++", "-O2", "-std=c++17", str(CSRC / "gen_instance.cpp"), "-o", str(GEN)]
 
@@ -95,7 +105,8 @@ def build(verbose: bool = False) -> None:
     """Compile the library, the drivers and the generator for sm_103a."""
     lib_in = lib_sources()
     OBJ_DIR.mkdir(exist_ok=True)
-    units = [u for u in LIB_UNITS if _stale(_obj(u), lib_in)]
+    headers = sorted(CSRC.glob("*.cuh")) + [INCLUDE / "segsort.h"]
+    units = [u for u in LIB_UNITS if _stale(_obj(u), [CSRC / u, *headers])]
     with ThreadPoolExecutor(max_workers=max(1, len(units))) as ex:
         for f in [ex.submit(_run, _obj_cmd(u), verbose) for u in units]:
             f.result()
@@ -109,6 +120,8 @@ def build(verbose: bool = False) -> None:
         jobs.append(_driver_cmd(DRIVER_TIME, True))
     if _stale(GEN, [CSRC / "gen_instance.cpp"]):
         jobs.append(_gen_cmd())
+    if _stale(SERVE, [CSRC / "serve_bench.cpp", INCLUDE / "segsort.h", LIB]):
+        jobs.append(_serve_cmd())
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for f in [ex.submit(_run, j, verbose) for j in jobs]:
             f.result()

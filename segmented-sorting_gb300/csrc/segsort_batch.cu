@@ -364,3 +364,9 @@ void segsort_batch_plan_destroy(segsort_batch_plan plan) {
 }
 
 }  // extern "C"
+
+extern "C" size_t segsort_batch_workspace_bytes(const segsort_batch_item *items, int32_t count) {
+  segsort::BatchLayout B;
+  if (segsort::build_layout(items, count, B) != SEGSORT_OK) return 0;
+  return B.total;
+}

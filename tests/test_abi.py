@@ -128,3 +128,27 @@ def test_batch_host_side_argument_checks(pkg):
     assert L.segsort_batch_plan_workspace_bytes(None) == 0
     L.segsort_batch_plan_destroy(None)
     del P
+
+
+def test_server_host_side_argument_checks(pkg):
+    """Server entry points reject bad arguments before any CUDA call."""
+    L = pkg.lib()
+    h = ctypes.c_void_p()
+    assert L.segsort_server_create(0, 0, 0, 0, ctypes.byref(h)) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_create(1 << 30, -1, 0, 0, ctypes.byref(h)) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_create(1 << 30, 0, -1, 0, ctypes.byref(h)) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_create(1 << 30, 0, 0, 9, ctypes.byref(h)) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_create(1 << 30, 0, 0, 0, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    t = ctypes.c_uint64()
+    assert L.segsort_server_submit(None, None, None, 0, None, 0, None, None,
+                                   ctypes.byref(t)) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_wait(None, 0, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_drain(None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_server_get_stats(None, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    L.segsort_server_destroy(None)
+    # the batch workspace query is host arithmetic
+    items = (pkg.BatchItem * 2)(pkg.BatchItem(0, 0, 16, 16, 1 << 20, 16, 4, 0),
+                                pkg.BatchItem(3, 0, 16, 16, 5000, 16, 2, 0))
+    ws = L.segsort_batch_workspace_bytes(items, 2)
+    assert ws > L.segsort_workspace_bytes(1 << 20, 4, 4, 4)
+    assert L.segsort_batch_workspace_bytes(items, -1) == 0
