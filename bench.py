@@ -496,7 +496,7 @@ def run_ours(args) -> None:
         ms_sum = sum(phase[lg]["tile_ms"] for lg in lens_in)
         launches = len(lens_in)
     else:
-        name = "large_sort_kernel"
+        name = "merge_sort_kernel"
         lens_in = [lg for lg in lengths if (1 << lg) > cap]
         ms_sum = sum(phase[lg]["large_ms"] for lg in lens_in)
         launches = len(lens_in)

@@ -1,0 +1,177 @@
+// Segment classification and the pieces the cooperative long-segment kernel
+// shares with the host: the workspace views, the counters, the bounded grid
+// barrier and the mapping of a job's instance to its buffers.
+//
+// Classify (one thread per segment boundary) replaces the reference's length
+// binning bb_bin (src/bb_segsort/bb_bin.h:23,31-139): instead of 13
+// power-of-two bins and a device-to-host copy of their counts (bb_bin.h:46),
+// it writes a half-tile -> first-segment map that the tile sort reads
+// directly, and a device-side list of the segments longer than the tile
+// capacity for the merge passes.
+#pragma once
+
+#include "segsort_common.cuh"
+
+namespace segsort {
+
+constexpr int kBarrierSpinLimit = 1 << 24;  // ~2 s with the back-off below
+
+enum : int {
+  kCtrJobs = 0,      // long segments found by classify
+  kCtrItems = 2,     // merge items of all jobs
+  kCtrPasses = 3,    // most merge passes of any job
+  kCtrBarCount = 6,  // grid barrier: arrivals
+  kCtrBarGen = 7,    // grid barrier: generation
+  kCtrWords = 16,
+};
+
+// Device views of the workspace.
+template <typename K>
+struct LargeWs {
+  uint32_t *ctr;          // [kCtrWords]
+  int4 *jobs;             // [max_jobs] long segments: {begin, end, 0, instance}
+  int32_t *item_prefix;   // [max_jobs + 1] merge items before each job
+  int32_t *half_first;    // [halves + 1] first segment starting at or after h * CAP/2
+  int32_t *item_job;      // [max_items] job of each merge item
+  uint32_t *split;        // [max_items] merge-path split of each item's first output
+  int4 *item_desc;        // [2 * max_items] item descriptors of the current pass
+  K *tmp_keys;            // [n]
+  uint32_t *tmp_vals;     // [n]
+  int32_t max_jobs;
+  int64_t max_items;
+  int64_t halves;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
+  return *reinterpret_cast<const volatile uint32_t *>(p);
+}
+
+// ---------------------------------------------------------------------------
+// Classify: one thread per segment boundary s in [0, nseg].
+//  * half_first[h] = s for every half-tile h with off(s-1) < h*half <= off(s)
+//    (off(-1) = -inf, off(nseg) = +inf): the first segment starting in or
+//    after half-tile h, so the tile sort needs no search over the offsets;
+//  * segments longer than cap become jobs of the merge passes (warp-aggregated
+//    atomic append), tagged with the instance they belong to.
+// Every lane of the warp calls it; `valid` is false for lanes past the end.
+template <typename K>
+__device__ __forceinline__ void classify_boundary(const Offsets &off, int64_t s, bool valid,
+                                                  int64_t cap, int64_t half, int32_t *half_first,
+                                                  int64_t halves, const LargeWs<K> &ws,
+                                                  int32_t inst) {
+  const int lane = threadIdx.x & 31;
+  int64_t len = 0, cur = 0;
+  if (valid && s <= off.nseg) {
+    cur = s < off.nseg ? off(s) : 0;
+    const int64_t h_lo = s == 0 ? 0 : off(s - 1) / half + 1;
+    const int64_t h_hi = s == off.nseg ? halves : min(cur / half, halves);
+    for (int64_t h = h_lo; h <= h_hi; ++h) half_first[h] = static_cast<int32_t>(s);
+    if (s < off.nseg) len = off(s + 1) - cur;
+  }
+  const bool large = len > cap;
+  const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, large);
+  if (ballot == 0) return;
+  uint32_t base = 0;
+  if (lane == 0) base = atomicAdd(&ws.ctr[kCtrJobs], __popc(ballot));
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  const uint32_t j = base + __popc(ballot & lanemask_lt());
+  if (large && j < static_cast<uint32_t>(ws.max_jobs))
+    ws.jobs[j] = make_int4(static_cast<int32_t>(cur), static_cast<int32_t>(cur + len), 0, inst);
+}
+
+template <typename K>
+__global__ void __launch_bounds__(256)
+large_classify_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
+  const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  classify_boundary<K>(off, s, true, cap, half, ws.half_first, ws.halves, ws, 0);
+}
+
+// Batched form: thread g classifies boundary g - bound_base of the instance
+// that owns it; `bounds` is the batch's total of nseg + 1 over its instances.
+template <typename K>
+__global__ void __launch_bounds__(256)
+large_classify_batch_kernel(const BatchInst *__restrict__ tab, int32_t count, int64_t bounds,
+                            int64_t cap, int64_t half, LargeWs<K> ws) {
+  const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool valid = g < bounds;
+  const int32_t i = find_instance(tab, count, valid ? g : 0, &BatchInst::bound_base);
+  const BatchInst &I = tab[i];
+  const int64_t tiles = (I.n + cap - 1) / cap;
+  classify_boundary<K>(I.offsets_view(), g - I.bound_base, valid, cap, half,
+                       ws.half_first + I.half_base, 2 * tiles, ws, i);
+}
+
+// ---------------------------------------------------------------------------
+// Where the long-segment kernel finds an instance's keys and values: the
+// caller's buffers and the instance's region of the temporary buffers, both
+// indexed by instance-local positions.
+template <typename K>
+struct SideBuffers {
+  K *keys;
+  uint32_t *vals;
+  K *tmp_keys;
+  uint32_t *tmp_vals;
+};
+
+// One problem: every job belongs to it.
+template <typename K>
+struct SingleSpace {
+  K *keys;
+  uint32_t *vals;
+  K *tmp_keys;
+  uint32_t *tmp_vals;
+  __device__ __forceinline__ SideBuffers<K> operator()(int32_t) const {
+    return {keys, vals, tmp_keys, tmp_vals};
+  }
+};
+
+// A batch: jobs carry their instance, whose buffers come from the table.
+template <typename K>
+struct BatchSpace {
+  const BatchInst *tab;
+  K *tmp_keys;
+  uint32_t *tmp_vals;
+  __device__ __forceinline__ SideBuffers<K> operator()(int32_t i) const {
+    const BatchInst &I = tab[i];
+    return {static_cast<K *>(I.keys), I.vals, tmp_keys + I.tmp_base,
+            tmp_vals ? tmp_vals + I.tmp_base : nullptr};
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Grid barrier for a cooperative launch (all CTAs resident), bounded: a CTA
+// that waits longer than kBarrierSpinLimit back-offs raises kStatusTimeout
+// and goes on, so a lost arrival can corrupt the result but never hang the
+// GPU.
+__device__ __forceinline__ void grid_barrier(uint32_t *ctr) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t gen = ld_volatile(ctr + kCtrBarGen);
+    __threadfence();
+    const uint32_t arrived = atomicAdd(ctr + kCtrBarCount, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(ctr + kCtrBarCount, 0u);
+      __threadfence();
+      atomicAdd(ctr + kCtrBarGen, 1u);
+    } else {
+      int spins = 0;
+      while (ld_volatile(ctr + kCtrBarGen) == gen) {
+        if (++spins > kBarrierSpinLimit) {
+          raise_status(kStatusTimeout);
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+}  // namespace segsort

@@ -68,7 +68,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // ---- one tile: every segment fits, no workspace, one kernel ---------------
   if (tiles == 1) {
     if (prof) rec.t0 = prof_event(stream);
-    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr);
+    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr, nullptr, nullptr);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     if (prof) {
       rec.t1 = prof_event(stream);
@@ -107,43 +107,48 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     const unsigned cls_blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 1 + 255) / 256);
     large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
 
-    // ---- long segments: one cooperative kernel (returns at once if none) -----
-    using LCfg = typename LargeFor<K, PAIRS>::Cfg;
-    using LS = LargeSmem<K, PAIRS, LCfg>;
-    auto large_kernel = large_sort_kernel<K, PAIRS, LCfg, SingleSpace<K>>;
-    static std::atomic<uint64_t> large_attr_done{0};
-    static std::atomic<int> large_occ[kMaxDevices];
-    if (!S->coop || ensure_smem(large_kernel, LS::kBytes, large_attr_done, dev) != cudaSuccess) {
+    // ---- tile sort: every segment of at most CAP elements, and the sorted
+    // CAP-runs of the longer ones -------------------------------------------------
+    if (prof) rec.t0 = prof_event(stream);
+    tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
+        keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals);
+    if (prof) rec.t1 = prof_event(stream);
+    if (cudaGetLastError() != cudaSuccess) {
       rc = SEGSORT_ERR_CUDA;
       break;
     }
-    // All resident CTAs, but no more than one per scatter chunk of the whole
+
+    // ---- long segments: merge passes in one cooperative kernel (returns at
+    // once without long segments) ----------------------------------------------------
+    using MS = MergeSmem<K, PAIRS>;
+    auto merge_kernel = merge_sort_kernel<K, PAIRS, SingleSpace<K>>;
+    static std::atomic<uint64_t> merge_attr_done{0};
+    static std::atomic<int> merge_occ[kMaxDevices];
+    if (!S->coop || ensure_smem(merge_kernel, MS::kBytes, merge_attr_done, dev) != cudaSuccess) {
+      rc = SEGSORT_ERR_CUDA;
+      break;
+    }
+    // All resident CTAs, but no more than one per merge item of the whole
     // problem: small calls then leave the rest of the GPU to other work.
-    const int lo = occupancy(large_kernel, kLThreads, LS::kBytes, large_occ, dev);
-    const int64_t chunks = (n + PassShape<K>::kChunk - 1) / PassShape<K>::kChunk;
-    const unsigned large_grid =
-        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, chunks));
+    const int mo = occupancy(merge_kernel, kMThreads, MS::kBytes, merge_occ, dev);
+    const int64_t items = n / MergeShape<K>::T + 1;
+    const unsigned merge_grid =
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(mo) * S->sms, items));
     if (prof) rec.l0 = prof_event(stream);
     {
       SingleSpace<K> sp{keys, vals, W.tmp_keys, W.tmp_vals};
-      void *args[] = {&sp, &W};
-      if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(large_kernel), dim3(large_grid),
-                                      dim3(kLThreads), args, LS::kBytes, stream) != cudaSuccess) {
+      int64_t cap = tile_cap<K>();
+      void *args[] = {&sp, &W, &cap};
+      if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(merge_kernel), dim3(merge_grid),
+                                      dim3(kMThreads), args, MS::kBytes, stream) != cudaSuccess) {
         rc = SEGSORT_ERR_CUDA;
         break;
       }
     }
     if (prof) rec.l1 = prof_event(stream);
-
-    // ---- tile sort: every segment of at most CAP elements -----------------------
-    if (prof) rec.t0 = prof_event(stream);
-    tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
-        keys, vals, off, W.half_first);
-    if (prof) rec.t1 = prof_event(stream);
-    if (cudaGetLastError() != cudaSuccess) rc = SEGSORT_ERR_CUDA;
   } while (false);
   if (prof) {
-    rec.large_launches = 2;  // classify, the cooperative long-segment kernel
+    rec.large_launches = 2;  // classify, the cooperative merge-pass kernel
     std::lock_guard<std::mutex> lk(g_prof_mu);
     g_prof_pending.push_back(rec);
   }
@@ -164,7 +169,7 @@ size_t workspace_bytes_for(int64_t n) {
 // device address; its address is looked up once per device.
 constexpr int64_t kNoAllocMaxN = SEGSORT_NOALLOC_MAX_N;
 constexpr size_t kNoAllocBytes =
-    make_layout(kNoAllocMaxN, 4, 4, tile_cap<uint32_t>(), PassShape<uint32_t>::kChunk).total;
+    make_layout(kNoAllocMaxN, 4, 4, tile_cap<uint32_t>(), MergeShape<uint32_t>::T).total;
 static_assert(kNoAllocBytes > 0, "the no-allocation scratch must cover the long-segment path");
 
 struct NoAllocScratch {

@@ -1,11 +1,11 @@
 // Batched form of the segmented sort: segsort_pairs_batch and batch plans.
 //
 // The instances of a batch are grouped by key type.  A group is sorted by the
-// same three kernels as one plain call -- classify, the cooperative
-// long-segment kernel, the tile sort -- launched once for the whole group:
-// every kernel finds an instance through a device table (BatchInst), tile-sort
-// CTAs and classify threads by binary search over the instances' bases, and
-// long-segment jobs through the instance index they carry.  Small instances
+// same three kernels as one plain call -- classify, the tile sort, the
+// cooperative merge passes for long segments -- launched once for the whole
+// group: every kernel finds an instance through a device table (BatchInst),
+// tile-sort CTAs and classify threads by binary search over the instances'
+// bases, and long-segment jobs through the instance index they carry.  Small instances
 // therefore share CTAs' worth of work with large ones instead of paying a
 // sequence of launches and grid barriers each.
 //
@@ -51,8 +51,8 @@ int64_t cap_of(int type) {
   return type == SEGSORT_KEY_U64 ? tile_cap<uint64_t>() : tile_cap<uint32_t>();
 }
 
-int64_t chunk_of(int type) {
-  return type == SEGSORT_KEY_U64 ? PassShape<uint64_t>::kChunk : PassShape<uint32_t>::kChunk;
+int64_t item_of(int type) {
+  return type == SEGSORT_KEY_U64 ? MergeShape<uint64_t>::T : MergeShape<uint32_t>::T;
 }
 
 // Validates the items and lays out every group.  Empty items (n == 0 or
@@ -94,7 +94,7 @@ int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B)
   for (int t = 0; t < kKeyTypes; ++t) {
     Group &G = g[t];
     if (G.insts.empty()) continue;
-    G.L = make_layout(G.total_n, key_bytes_of(t), 4, cap_of(t), chunk_of(t), G.half_entries);
+    G.L = make_layout(G.total_n, key_bytes_of(t), 4, cap_of(t), item_of(t), G.half_entries);
     G.tab_off = off;
     off = align256(off + G.insts.size() * sizeof(BatchInst));
     G.ws_off = off;
@@ -138,20 +138,19 @@ cudaError_t upload_table(const std::vector<BatchInst> &v, BatchInst *dst, cudaSt
 template <typename K>
 struct BatchKernels {
   using TCfg = typename TileFor<K, true>::Cfg;
-  using LCfg = typename LargeFor<K, true>::Cfg;
-  using LS = LargeSmem<K, true, LCfg>;
+  using MS = MergeSmem<K, true>;
   static constexpr auto tile = tile_sort_batch_kernel<K, true, TCfg::NT, TCfg::KPT,
                                                       TileFor<K, true>::kMinBlocks>;
-  static constexpr auto large = large_sort_kernel<K, true, LCfg, BatchSpace<K>>;
+  static constexpr auto merge = merge_sort_kernel<K, true, BatchSpace<K>>;
   static constexpr auto classify = large_classify_batch_kernel<K>;
-  static inline std::atomic<uint64_t> tile_attr{0}, large_attr{0};
-  static inline std::atomic<int> large_occ[kMaxDevices];
+  static inline std::atomic<uint64_t> tile_attr{0}, merge_attr{0};
+  static inline std::atomic<int> merge_occ[kMaxDevices];
 
   // Attributes and occupancy, before any capture.
   static cudaError_t prepare(int dev) {
     cudaError_t e = ensure_smem(tile, TCfg::kSmemBytes, tile_attr, dev);
-    if (e == cudaSuccess) e = ensure_smem(large, LS::kBytes, large_attr, dev);
-    if (e == cudaSuccess) occupancy(large, kLThreads, LS::kBytes, large_occ, dev);
+    if (e == cudaSuccess) e = ensure_smem(merge, MS::kBytes, merge_attr, dev);
+    if (e == cudaSuccess) occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     return e;
   }
 
@@ -167,26 +166,26 @@ struct BatchKernels {
     classify<<<cls_blocks, 256, 0, stream>>>(tab, count, G.bounds, cap, cap / 2, W);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
 
-    const int lo = occupancy(large, kLThreads, LS::kBytes, large_occ, dev);
-    const int64_t chunks = (G.total_n + PassShape<K>::kChunk - 1) / PassShape<K>::kChunk;
+    // Tile sort first: it forms the sorted runs the merge passes read.
+    tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, TCfg::kSmemBytes, stream>>>(
+        tab, count, W.half_first, W.tmp_keys, W.tmp_vals);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
+    const int64_t items = G.total_n / MergeShape<K>::T + 1;
     const unsigned grid =
-        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S.sms, chunks));
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(mo) * S.sms, items));
     BatchSpace<K> sp{tab, W.tmp_keys, W.tmp_vals};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kLThreads);
-    cfg.dynamicSmemBytes = LS::kBytes;
+    cfg.blockDim = dim3(kMThreads);
+    cfg.dynamicSmemBytes = MS::kBytes;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (cudaLaunchKernelEx(&cfg, large, sp, W) != cudaSuccess) return SEGSORT_ERR_CUDA;
-
-    tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, TCfg::kSmemBytes, stream>>>(tab, count,
-                                                                                W.half_first);
-    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    if (cudaLaunchKernelEx(&cfg, merge, sp, W, cap) != cudaSuccess) return SEGSORT_ERR_CUDA;
     return SEGSORT_OK;
   }
 };

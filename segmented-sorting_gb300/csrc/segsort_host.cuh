@@ -14,7 +14,8 @@
 #include "segsort.h"
 #include "segsort_common.cuh"
 #include "tile_sort.cuh"
-#include "large_sort.cuh"
+#include "classify.cuh"
+#include "merge_sort.cuh"
 
 namespace segsort {
 
@@ -41,43 +42,31 @@ constexpr int64_t tile_cap() {
   return TileFor<K, false>::Cfg::CAP;
 }
 
-// Bucket-sort shape of the long-segment kernel: its 512-thread CTAs sort
-// chunks of 8192 (32-bit keys) or 4096 (64-bit keys) elements.
-template <typename K, bool PAIRS>
-struct LargeFor {
-  using Cfg = TileConfig<K, PAIRS, kLThreads, sizeof(K) == 4 ? 16 : 8>;
-};
-
 // ---------------------------------------------------------------------------
 // Workspace layout (every region 256-byte aligned).
 struct WsLayout {
-  size_t ctr = 0, jobs0 = 0, jobs1 = 0, prefix = 0, hist = 0, bstart = 0, digit = 0, status = 0,
-         desc = 0, entries = 0, half_first = 0, tmp_keys = 0, tmp_vals = 0;
+  size_t ctr = 0, jobs = 0, prefix = 0, half_first = 0, item_job = 0, split = 0, item_desc = 0,
+         tmp_keys = 0, tmp_vals = 0;
   size_t total = 0;
   int32_t max_jobs = 0;
-  int64_t max_chunks = 0;
-  int64_t max_entries = 0;
+  int64_t max_items = 0;
   int64_t halves = 0;
-  int passes = 0;
 };
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
-// half_entries: entries of the half-tile map (default: one problem of n
-// elements, 2 * tiles + 1); a batch passes the sum over its instances and
-// always needs the workspace.
+// item: outputs per merge item.  half_entries: entries of the half-tile map
+// (default: one problem of n elements, 2 * tiles + 1); a batch passes the sum
+// over its instances and always needs the workspace.
 constexpr WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t cap,
-                               int64_t chunk, int64_t half_entries = -1) {
+                               int64_t item, int64_t half_entries = -1) {
   WsLayout L;
   if (n <= cap && half_entries < 0) return L;  // one tile: no workspace
-  // Jobs of every level are longer than cap: at most n / (cap + 1) of them.
+  // Jobs are longer than cap: at most n / (cap + 1) of them.
   L.max_jobs = static_cast<int32_t>(n / (cap + 1) + 1);
-  L.max_chunks = n / chunk + L.max_jobs + 1;
-  // Bucket chunks: greedy packing gives at most 4 len / cap + 1 per job,
-  // copies at most len / cap + 1.
-  L.max_entries = 5 * (n / cap) + 2 * static_cast<int64_t>(L.max_jobs) + 16;
+  // Merge items: ceil(len / item) per job.
+  L.max_items = n / item + L.max_jobs + 1;
   L.halves = half_entries < 0 ? 2 * ((n + cap - 1) / cap) : half_entries - 1;
-  L.passes = key_bytes;  // 8-bit digits
   size_t off = 0;
   auto take = [&off](size_t bytes) {
     const size_t at = off;
@@ -85,17 +74,14 @@ constexpr WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t 
     return at;
   };
   const size_t mj = static_cast<size_t>(L.max_jobs);
+  const size_t mi = static_cast<size_t>(L.max_items);
   L.ctr = take(kCtrWords * sizeof(uint32_t));
-  L.jobs0 = take(mj * sizeof(int4));
-  L.jobs1 = take(mj * sizeof(int4));
+  L.jobs = take(mj * sizeof(int4));
   L.prefix = take((mj + 1) * 4);
-  L.hist = take(mj * L.passes * kRadix * 4);
-  L.bstart = take(mj * (kRadix + 1) * 4);
-  L.digit = take(mj * 4);
-  L.status = take(static_cast<size_t>(L.max_chunks) * kRadix * 4);
-  L.desc = take(static_cast<size_t>(L.max_chunks) * sizeof(int4));
-  L.entries = take(static_cast<size_t>(L.max_entries) * sizeof(int4));
   L.half_first = take(static_cast<size_t>(L.halves + 1) * 4);
+  L.item_job = take(mi * 4);
+  L.split = take(mi * 4);
+  L.item_desc = take(mi * 2 * sizeof(int4));
   L.tmp_keys = take(static_cast<size_t>(n) * key_bytes);
   L.tmp_vals = take(static_cast<size_t>(n) * val_bytes);
   L.total = off;
@@ -104,7 +90,7 @@ constexpr WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t 
 
 template <typename K, bool PAIRS>
 inline WsLayout layout_for(int64_t n) {
-  return make_layout(n, sizeof(K), PAIRS ? 4 : 0, tile_cap<K>(), PassShape<K>::kChunk);
+  return make_layout(n, sizeof(K), PAIRS ? 4 : 0, tile_cap<K>(), MergeShape<K>::T);
 }
 
 // Device views of a workspace laid out by make_layout at `base`.
@@ -112,22 +98,16 @@ template <typename K, bool PAIRS>
 inline LargeWs<K> ws_views(unsigned char *base, const WsLayout &L) {
   LargeWs<K> W;
   W.ctr = reinterpret_cast<uint32_t *>(base + L.ctr);
-  W.jobs[0] = reinterpret_cast<int4 *>(base + L.jobs0);
-  W.jobs[1] = reinterpret_cast<int4 *>(base + L.jobs1);
-  W.chunk_prefix = reinterpret_cast<int32_t *>(base + L.prefix);
-  W.hist = reinterpret_cast<uint32_t *>(base + L.hist);
-  W.bstart = reinterpret_cast<int32_t *>(base + L.bstart);
-  W.digit = reinterpret_cast<int32_t *>(base + L.digit);
-  W.status = reinterpret_cast<uint32_t *>(base + L.status);
-  W.desc = reinterpret_cast<int4 *>(base + L.desc);
-  W.entries = reinterpret_cast<int4 *>(base + L.entries);
+  W.jobs = reinterpret_cast<int4 *>(base + L.jobs);
+  W.item_prefix = reinterpret_cast<int32_t *>(base + L.prefix);
   W.half_first = reinterpret_cast<int32_t *>(base + L.half_first);
+  W.item_job = reinterpret_cast<int32_t *>(base + L.item_job);
+  W.split = reinterpret_cast<uint32_t *>(base + L.split);
+  W.item_desc = reinterpret_cast<int4 *>(base + L.item_desc);
   W.tmp_keys = reinterpret_cast<K *>(base + L.tmp_keys);
   W.tmp_vals = PAIRS ? reinterpret_cast<uint32_t *>(base + L.tmp_vals) : nullptr;
   W.max_jobs = L.max_jobs;
-  W.passes = L.passes;
-  W.max_chunks = L.max_chunks;
-  W.max_entries = L.max_entries;
+  W.max_items = L.max_items;
   W.halves = L.halves;
   return W;
 }

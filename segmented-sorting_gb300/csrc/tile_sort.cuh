@@ -688,22 +688,42 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
   write_chunk<Cfg, PAIRS>(w, m, smem, dst_keys, dst_vals);
 }
 
+// Merge passes a long segment of len elements needs after its CAP-runs are
+// sorted: ceil(log2(ceil(len / CAP))).
+__host__ __device__ __forceinline__ int merge_passes(int64_t len, int64_t cap) {
+  int p = 0;
+  for (int64_t runs = (len + cap - 1) / cap; runs > 1; runs = (runs + 1) >> 1) ++p;
+  return p;
+}
+
 // ---------------------------------------------------------------------------
 // One CTA of the tile sort: tile t of a problem whose half-tile map is
 // half_first (null: the problem is one tile, n <= CAP, and the CTA sorts one
 // chunk with every segment).
+//
+// With tmp_keys given, the CTA also forms the sorted runs of long segments
+// (longer than CAP) for the merge passes: every CAP-chunk [b + k*CAP, ...) of
+// such a segment is sorted by the CTA of the tile its first element lies in,
+// into the buffer the segment's first merge pass reads (the caller's
+// buffers when the segment needs an even number of passes, tmp otherwise, so
+// that its last pass writes the caller's buffers).  A tile holds at most one
+// such chunk of the segment running into it and the first chunk of at most
+// one long segment starting in each of its halves.
 // ---------------------------------------------------------------------------
 template <typename K, bool PAIRS, int NT, int KPT>
 __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restrict__ vals,
                                          const Offsets &off, const int32_t *__restrict__ half_first,
-                                         int64_t t) {
+                                         int64_t t, K *__restrict__ tmp_keys = nullptr,
+                                         uint32_t *__restrict__ tmp_vals = nullptr) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   constexpr int CAP = Cfg::CAP;
   constexpr int64_t HALF = Cfg::HALF;
+  constexpr int kMaxChunks = 5;
 
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int64_t chunk_s[4][3];  // a, lo, hi
-  __shared__ int32_t chunk_m[4];
+  __shared__ int64_t chunk_s[kMaxChunks][3];  // a, lo, hi (lo = hi: a long-segment run)
+  __shared__ int32_t chunk_m[kMaxChunks];
+  __shared__ int32_t chunk_tmp[kMaxChunks];   // the run goes to tmp
   __shared__ int nchunks_s;
   __shared__ uint32_t hb[CAP / 32];
   __shared__ int warp_s[NT / 32];
@@ -724,6 +744,19 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
       chunk_s[nc][1] = lo;
       chunk_s[nc][2] = hi;
       chunk_m[nc] = static_cast<int32_t>(m);
+      chunk_tmp[nc] = 0;
+      ++nc;
+    };
+    // The CAP-chunk of long segment s that starts at c.
+    auto add_run = [&](int64_t s, int64_t c) {
+      if (tmp_keys == nullptr) return;
+      const int64_t b = off(s), e = off(s + 1);
+      if (e - b <= CAP || c < b || c >= e) return;
+      chunk_s[nc][0] = c;
+      chunk_s[nc][1] = s;
+      chunk_s[nc][2] = s;
+      chunk_m[nc] = static_cast<int32_t>(min(static_cast<int64_t>(CAP), e - c));
+      chunk_tmp[nc] = merge_passes(e - b, CAP) & 1;
       ++nc;
     };
     if (half_first == nullptr) {
@@ -733,7 +766,16 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
       const int64_t h0 = clampi(__ldg(half_first + 2 * t), 0);
       const int64_t h1 = clampi(__ldg(half_first + 2 * t + 1), h0);
       const int64_t h2 = clampi(__ldg(half_first + 2 * t + 2), h1);
-      // A last segment of a half-tile longer than HALF is a chunk of its own.
+      // A long segment that starts before the tile and runs into it.
+      if (tmp_keys != nullptr && h0 > 0) {
+        const int64_t b = off(h0 - 1), e = off(h0), t0 = t * CAP;
+        if (e - b > CAP && b < t0 && e > t0) {
+          const int64_t c = b + (t0 - b + CAP - 1) / CAP * CAP;
+          if (c < e && c < t0 + CAP) add_run(h0 - 1, c);
+        }
+      }
+      // A last segment of a half-tile longer than HALF is a chunk of its own,
+      // or, when longer than CAP, a long segment whose first run starts here.
       const bool big_a = h1 > h0 && off(h1) - off(h1 - 1) > HALF;
       const bool big_b = h2 > h1 && off(h2) - off(h2 - 1) > HALF;
       const int64_t end_a = big_a ? h1 - 1 : h1;
@@ -742,10 +784,16 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
         add(h0, end_b);  // both halves' short segments in one chunk
       } else {
         add(h0, end_a);
-        if (big_a) add(h1 - 1, h1);
+        if (big_a) {
+          add(h1 - 1, h1);
+          add_run(h1 - 1, off(h1 - 1));
+        }
         add(h1, end_b);
       }
-      if (big_b) add(h2 - 1, h2);
+      if (big_b) {
+        add(h2 - 1, h2);
+        add_run(h2 - 1, off(h2 - 1));
+      }
     }
     nchunks_s = nc;
   }
@@ -755,7 +803,9 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
     const int64_t a = chunk_s[c][0], lo = chunk_s[c][1], hi = chunk_s[c][2];
     K *k = keys + a;
     uint32_t *v = PAIRS ? vals + a : nullptr;
-    sort_chunk<Cfg, PAIRS>(k, v, k, v, chunk_m[c], hi - lo > 1,
+    K *dk = chunk_tmp[c] ? tmp_keys + a : k;
+    uint32_t *dv = PAIRS ? (chunk_tmp[c] ? tmp_vals + a : v) : nullptr;
+    sort_chunk<Cfg, PAIRS>(k, v, dk, dv, chunk_m[c], hi - lo > 1,
                            [&](auto &&set) {
                              for (int64_t j = lo + tid; j < hi; j += NT) set(off(j) - a);
                            },
@@ -769,8 +819,9 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
 template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
-                 const int32_t *__restrict__ half_first) {
-  tile_cta<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x);
+                 const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
+                 uint32_t *__restrict__ tmp_vals) {
+  tile_cta<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x, tmp_keys, tmp_vals);
 }
 
 // ---------------------------------------------------------------------------
@@ -782,12 +833,14 @@ tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
 template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_sort_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
-                       const int32_t *__restrict__ half_first) {
+                       const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
+                       uint32_t *__restrict__ tmp_vals) {
   const int64_t t = blockIdx.x;
   const int32_t i = find_instance(tab, count, t, &BatchInst::tile_base);
   const BatchInst &I = tab[i];
   tile_cta<K, PAIRS, NT, KPT>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
-                              half_first + I.half_base, t - I.tile_base);
+                              half_first + I.half_base, t - I.tile_base, tmp_keys + I.tmp_base,
+                              PAIRS ? tmp_vals + I.tmp_base : nullptr);
 }
 
 }  // namespace segsort
