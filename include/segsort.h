@@ -143,7 +143,7 @@ int segsort_keys_u32_ws(uint32_t *d_keys, int64_t n, const int32_t *d_offsets,
  * or fail on, an allocation once running, and code that must not fail with
  * out-of-memory in mid-run.  The temporary storage is a fixed scratch array
  * that is part of the library's device code, sized for n up to
- * SEGSORT_NOALLOC_MAX_N uint32 key/value pairs (about 9.7 MiB); every GPU
+ * SEGSORT_NOALLOC_MAX_N uint32 key/value pairs (about 8 MiB); every GPU
  * that loads the library holds it until the process exits.  The call makes
  * no cudaMalloc, cudaFree or other allocating call.
  *
