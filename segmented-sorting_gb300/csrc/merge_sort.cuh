@@ -358,19 +358,28 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
                 lo = mid + 1;
               else hi = mid;
             }
+            // The heads of both windows stay in registers: one key and one
+            // value read from shared memory per output.
             int ai = lo, bi = dt - lo;
+            K av = Xk[MS::xslot(ai < wa ? ai : 0)];
+            K bv = Xk[MS::xslot(bi < wb ? wa + bi : 0)];
 #pragma unroll
             for (int q = 0; q < KPT; ++q) {
               const int pos = dt + q;
               if (pos < m) {
                 const bool take_a =
-                    ai < wa && (bi >= wb || Ord::to_bits(Xk[MS::xslot(ai)]) <=
-                                                Ord::to_bits(Xk[MS::xslot(wa + bi)]));
-                const int x = MS::xslot(take_a ? ai : wa + bi);
-                Ok[MS::oslot(pos)] = Xk[x];
-                if constexpr (PAIRS) Ov[MS::oslot(pos)] = Xv[x];
+                    ai < wa && (bi >= wb || Ord::to_bits(av) <= Ord::to_bits(bv));
+                const int x = take_a ? ai : wa + bi;
+                Ok[MS::oslot(pos)] = take_a ? av : bv;
+                if constexpr (PAIRS) Ov[MS::oslot(pos)] = Xv[MS::xslot(x)];
                 ai += take_a;
                 bi += !take_a;
+                // Next head of the side just consumed (any in-range slot when
+                // that side is exhausted: it is never compared again).
+                const int nx = take_a ? (ai < wa ? ai : 0) : (bi < wb ? wa + bi : 0);
+                const K nv = Xk[MS::xslot(nx)];
+                av = take_a ? nv : av;
+                bv = take_a ? bv : nv;
               }
             }
           }
