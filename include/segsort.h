@@ -161,6 +161,67 @@ int segsort_pairs_u32_noalloc(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
                               segsort_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Descending order, stable: equal keys keep their input order.  Replaces
+ * cub::DeviceSegmentedRadixSort::SortPairsDescending
+ * (lib/cub/device/device_segmented_radix_sort.cuh:338).  The keys are mapped
+ * in place to the complement of their order bits, sorted ascending and
+ * mapped back (two extra element-wise passes over the keys).
+ * ---------------------------------------------------------------------- */
+int segsort_pairs_u32_desc(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg,
+                           segsort_stream_t stream);
+int segsort_pairs_i32_desc(int32_t *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg,
+                           segsort_stream_t stream);
+int segsort_pairs_f32_desc(float *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg,
+                           segsort_stream_t stream);
+int segsort_pairs_u64_desc(uint64_t *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg,
+                           segsort_stream_t stream);
+int segsort_keys_u32_desc(uint32_t *d_keys, int64_t n, const int32_t *d_offsets,
+                          int32_t nseg, segsort_stream_t stream);
+int segsort_keys_f32_desc(float *d_keys, int64_t n, const int32_t *d_offsets,
+                          int32_t nseg, segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Segmented top-k (no reference counterpart).  Sorts every segment in place
+ * (ascending, or stable descending when `descending` is non-zero), then
+ * writes its first min(k, len) keys -- and values, when d_out_vals is not
+ * null -- to row s of the [nseg][k] outputs, and min(k, len) to
+ * d_out_counts[s] when d_out_counts is not null.  Output slots past a row's
+ * count are not written.
+ * ---------------------------------------------------------------------- */
+int segsort_pairs_u32_topk(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg, int64_t k,
+                           int descending, uint32_t *d_out_keys,
+                           uint32_t *d_out_vals, int32_t *d_out_counts,
+                           segsort_stream_t stream);
+int segsort_pairs_f32_topk(float *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg, int64_t k,
+                           int descending, float *d_out_keys, uint32_t *d_out_vals,
+                           int32_t *d_out_counts, segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 64-bit values (the reference's bb_segsort instances carry double values,
+ * src/bb_segsort/main.cu:68-72).  The keys are sorted with their positions
+ * as 32-bit values, then the 64-bit values are gathered through those
+ * positions (workspace: 12 bytes per element from the library's pool).
+ * ---------------------------------------------------------------------- */
+int segsort_pairs_u32_v64(uint32_t *d_keys, uint64_t *d_vals, int64_t n,
+                          const int32_t *d_offsets, int32_t nseg,
+                          segsort_stream_t stream);
+int segsort_pairs_i32_v64(int32_t *d_keys, uint64_t *d_vals, int64_t n,
+                          const int32_t *d_offsets, int32_t nseg,
+                          segsort_stream_t stream);
+int segsort_pairs_f32_v64(float *d_keys, uint64_t *d_vals, int64_t n,
+                          const int32_t *d_offsets, int32_t nseg,
+                          segsort_stream_t stream);
+int segsort_pairs_u64_v64(uint64_t *d_keys, uint64_t *d_vals, int64_t n,
+                          const int32_t *d_offsets, int32_t nseg,
+                          segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Batched form: many independent instances, each with its own keys, uint32
  * values and offsets, sorted by one launch of each kernel per key type
  * instead of one sequence of launches per instance.  No counterpart in the

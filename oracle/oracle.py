@@ -105,14 +105,22 @@ def segsort_cpp(keys: np.ndarray, offsets: np.ndarray, vals: np.ndarray | None =
     return k, v
 
 
-def segsort_numpy(keys: np.ndarray, offsets: np.ndarray, vals: np.ndarray | None = None):
-    """Same result as segsort_cpp via one stable lexsort.  Returns new arrays."""
+def segsort_numpy(keys: np.ndarray, offsets: np.ndarray, vals: np.ndarray | None = None,
+                  descending: bool = False):
+    """Same result as segsort_cpp via one stable lexsort.  Returns new arrays.
+
+    descending=True sorts every segment by decreasing key, equal keys in input
+    order (the stable descending order of CUB's SortPairsDescending,
+    lib/cub/device/device_segmented_radix_sort.cuh:338).  Values keep their
+    dtype (32- or 64-bit)."""
     n = len(keys)
     o = np.clip(np.asarray(offsets, dtype=np.int64), 0, n)
     b, e = o[:-1], o[1:]
     lens = np.maximum(e - b, 0)
     k = np.array(keys, copy=True)
-    v = None if vals is None else np.array(vals, dtype=np.uint32, copy=True)
+    if vals is not None and np.asarray(vals).dtype not in (np.dtype(np.uint32), np.dtype(np.uint64)):
+        vals = np.asarray(vals, dtype=np.uint32)
+    v = None if vals is None else np.array(vals, copy=True)
     if n == 0 or lens.sum() == 0:
         return k if v is None else (k, v)
     # Positions covered by a segment, in segment order, and their segment ids.
@@ -121,10 +129,12 @@ def segsort_numpy(keys: np.ndarray, offsets: np.ndarray, vals: np.ndarray | None
     within = np.arange(len(seg_ids), dtype=np.int64) - np.repeat(np.cumsum(lens) - lens, lens)
     pos = starts + within
     bits = order_bits(keys[pos])
+    if descending:
+        bits = ~bits
     order = np.lexsort((bits, seg_ids))  # stable: ties keep position order
     k[pos] = keys[pos][order]
     if v is not None:
-        v[pos] = np.asarray(vals, dtype=np.uint32)[pos][order]
+        v[pos] = np.asarray(vals)[pos][order]
         return k, v
     return k
 

@@ -62,6 +62,12 @@ SIGNATURES = {
     "segsort_pairs_u32_ws": ([_P, _P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "segsort_keys_u32_ws": ([_P, _I64, _P, _I32, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "segsort_pairs_u32_noalloc": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int),
+    **{f"segsort_pairs_{t}_desc": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int) for t in KEY_TYPES},
+    "segsort_keys_u32_desc": ([_P, _I64, _P, _I32, _P], ctypes.c_int),
+    "segsort_keys_f32_desc": ([_P, _I64, _P, _I32, _P], ctypes.c_int),
+    **{f"segsort_pairs_{t}_topk": ([_P, _P, _I64, _P, _I32, _I64, ctypes.c_int, _P, _P, _P, _P],
+                                   ctypes.c_int) for t in ("u32", "f32")},
+    **{f"segsort_pairs_{t}_v64": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int) for t in KEY_TYPES},
     "segsort_pairs_batch": ([ctypes.POINTER(BatchItem), _I32, _P], ctypes.c_int),
     "segsort_batch_plan_create": ([ctypes.POINTER(BatchItem), _I32, ctypes.POINTER(_P)], ctypes.c_int),
     "segsort_batch_plan_launch": ([_P, _P], ctypes.c_int),

@@ -3,7 +3,9 @@
 Products, all written next to this file:
   libsegsort.so          the C-ABI library (csrc/segsort_api.cu: plain calls,
                          csrc/segsort_batch.cu: batched form,
-                         csrc/segsort_server.cu: served form; sm_103a)
+                         csrc/segsort_server.cu: served form,
+                         csrc/segsort_ext.cu: descending, top-k, 64-bit
+                         values; sm_103a)
   serve_bench.exe        served-form benchmark driver (Poisson request stream)
   segsort_driver.exe     reference-compatible bench driver, prints sorted keys
   segsort_driver_time.exe  the same driver built with ELAPSED_TIME=1
@@ -62,7 +64,7 @@ def _run(cmd: list[str], verbose: bool) -> None:
 
 
 OBJ_DIR = PKG / "_build"
-LIB_UNITS = ["segsort_api.cu", "segsort_batch.cu", "segsort_server.cu"]
+LIB_UNITS = ["segsort_api.cu", "segsort_batch.cu", "segsort_server.cu", "segsort_ext.cu"]
 
 
 def _obj(unit: str) -> Path:

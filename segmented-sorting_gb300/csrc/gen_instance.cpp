@@ -8,7 +8,8 @@
 // Invoked through a link named equal.exe or diff.exe, the first word may be
 // omitted, so scripts/genequalseg.sh and scripts/gendiffseg.sh run unchanged.
 //
-// Options: --bits B (keys uniform in [0, 2^B), default 12 as utils/Makefile:1;
+// Options: --binary (write the binary instance format of segsort_driver.cpp),
+//          --bits B (keys uniform in [0, 2^B), default 12 as utils/Makefile:1;
 //          B = 32 for the full range), --seed S (default 1), --order
 //          rand|asc|desc|randminmax (utils/gen_equal.cpp:18-92),
 //          --mu M --sigma S --max L --empty F (lognormal lengths).
@@ -51,9 +52,33 @@ uint64_t key_of(uint64_t seed, uint64_t i, int bits) {
 void usage() {
   std::fprintf(stderr,
                "usage: gen_instance.exe equal <nseg> <segment_size> | diff <nseg> <n> | "
-               "lognormal <n>  [--bits B] [--seed S] [--order rand|asc|desc|randminmax] "
+               "lognormal <n>  [--binary] [--bits B] [--seed S] [--order rand|asc|desc|randminmax] "
                "[--mu M] [--sigma S] [--max L] [--empty F]\n");
   std::exit(1);
+}
+
+// Binary instance (read by segsort_driver.exe): 32-byte header {"SGSB",
+// version 1, key bytes, key kind 0 = unsigned, nseg, n}, nseg+1 int32
+// offsets, zero padding to a multiple of 8 bytes, n little-endian keys
+// (uint32 for bits <= 32, uint64 otherwise).
+void emit_binary(const std::vector<int64_t> &off, const std::vector<uint64_t> &keys, int bits) {
+  const uint32_t key_bytes = bits <= 32 ? 4 : 8;
+  const uint32_t head[4] = {0, 1, key_bytes, 0};
+  const uint64_t counts[2] = {off.size() - 1, keys.size()};
+  std::fwrite("SGSB", 1, 4, stdout);
+  std::fwrite(head + 1, 4, 3, stdout);
+  std::fwrite(counts, 8, 2, stdout);
+  std::vector<int32_t> o32(off.begin(), off.end());
+  std::fwrite(o32.data(), 4, o32.size(), stdout);
+  const size_t pad = (8 - (32 + o32.size() * 4) % 8) % 8;
+  const char zeros[8] = {0};
+  std::fwrite(zeros, 1, pad, stdout);
+  if (key_bytes == 4) {
+    std::vector<uint32_t> k32(keys.begin(), keys.end());
+    std::fwrite(k32.data(), 4, k32.size(), stdout);
+  } else {
+    std::fwrite(keys.data(), 8, keys.size(), stdout);
+  }
 }
 
 void emit(const std::vector<int64_t> &off, const std::vector<uint64_t> &keys) {
@@ -83,6 +108,7 @@ int main(int argc, char **argv) {
   int bits = 12;
   uint64_t seed = 1;
   std::string order = "rand";
+  bool binary = false;
   double mu = 4.0, sigma = 2.5, empty_frac = 0.01;
   int64_t max_len = int64_t{1} << 22;
   std::vector<std::string> pos;
@@ -92,7 +118,8 @@ int main(int argc, char **argv) {
       if (i + 1 >= args.size()) usage();
       return args[++i];
     };
-    if (a == "--bits") bits = std::atoi(val().c_str());
+    if (a == "--binary") binary = true;
+    else if (a == "--bits") bits = std::atoi(val().c_str());
     else if (a == "--seed") seed = std::strtoull(val().c_str(), nullptr, 10);
     else if (a == "--order") order = val();
     else if (a == "--mu") mu = std::atof(val().c_str());
@@ -177,6 +204,7 @@ int main(int argc, char **argv) {
   } else if (order != "rand") {
     usage();
   }
-  emit(off, keys);
+  if (binary) emit_binary(off, keys, bits);
+  else emit(off, keys);
   return 0;
 }

@@ -14,6 +14,14 @@
 // run against it unchanged.  ELAPSED_TIME and EXECUTIONS are compile-time
 // defaults (as in src/Makefile:11-86) that the options below override.
 //
+// Binary instances (gen_instance.exe --binary) are read as well: a file that
+// starts with the magic "SGSB" holds a 32-byte header (magic, version 1, key
+// bytes 4 or 8, key kind 0 unsigned / 1 signed / 2 float, nseg and n as
+// uint64), the nseg+1 int32 offsets, zero padding to a multiple of 8 bytes
+// and the n keys, all little-endian.  When stdin is a regular file it is
+// memory-mapped instead of read, and the keys are copied to the GPU straight
+// from the mapping; the key type comes from the header.
+//
 // Options:
 //   --pairs           sort (key, value) pairs with value = input index
 //                     (the convention of src/radixseg.cu:89); default keys only
@@ -28,6 +36,10 @@
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <cuda_runtime.h>
 
@@ -51,33 +63,62 @@ void check_cuda(cudaError_t e, const char *what) {
   if (e != cudaSuccess) die(what, cudaGetErrorString(e));
 }
 
-// Whole-stdin tokenizer (scanf is too slow for 2^25-key instances).
+// All of stdin: memory-mapped when it is a regular file, read otherwise.
+// Text instances are tokenised from it (scanf is too slow for 2^25-key
+// instances); binary instances are used in place.
 struct Reader {
   std::vector<char> buf;
+  const char *data = nullptr;
+  size_t size = 0;
+  void *map = nullptr;
   size_t pos = 0;
   Reader() {
+    struct stat st;
+    if (fstat(0, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0) {
+      map = mmap(nullptr, static_cast<size_t>(st.st_size), PROT_READ, MAP_PRIVATE, 0, 0);
+      if (map == MAP_FAILED) map = nullptr;
+      if (map) {
+        data = static_cast<const char *>(map);
+        size = static_cast<size_t>(st.st_size);
+        return;
+      }
+    }
     char tmp[1 << 16];
     size_t r;
     while ((r = std::fread(tmp, 1, sizeof(tmp), stdin)) > 0) buf.insert(buf.end(), tmp, tmp + r);
-    buf.push_back('\0');
+    data = buf.data();
+    size = buf.size();
   }
+  ~Reader() {
+    if (map) munmap(map, size);
+  }
+  bool binary() const { return size >= 32 && std::memcmp(data, "SGSB", 4) == 0; }
+  static bool space(char c) { return c == ' ' || c == '\n' || c == '\r' || c == '\t'; }
+  // Next token as a NUL-terminated copy (tokens are short numbers).
   const char *next() {
-    while (pos < buf.size() && (buf[pos] == ' ' || buf[pos] == '\n' || buf[pos] == '\r' ||
-                                buf[pos] == '\t'))
-      ++pos;
-    if (pos >= buf.size() - 1) return nullptr;
-    const char *s = &buf[pos];
-    while (pos < buf.size() && buf[pos] != ' ' && buf[pos] != '\n' && buf[pos] != '\r' &&
-           buf[pos] != '\t' && buf[pos] != '\0')
-      ++pos;
-    return s;
+    while (pos < size && space(data[pos])) ++pos;
+    if (pos >= size) return nullptr;
+    size_t len = 0;
+    while (pos < size && !space(data[pos]) && data[pos] != '\0' && len + 1 < sizeof(tok))
+      tok[len++] = data[pos++];
+    while (pos < size && !space(data[pos]) && data[pos] != '\0') ++pos;
+    tok[len] = '\0';
+    return tok;
   }
   long long next_int() {
     const char *s = next();
     if (!s) die("truncated input", nullptr);
     return std::strtoll(s, nullptr, 10);
   }
+  char tok[64];
 };
+
+struct BinaryHeader {
+  char magic[4];
+  uint32_t version, key_bytes, key_kind;
+  uint64_t nseg, n;
+};
+static_assert(sizeof(BinaryHeader) == 32, "binary instance header is 32 bytes");
 
 template <typename K>
 K parse_key(const char *s);
@@ -127,7 +168,24 @@ struct Opts {
 };
 
 template <typename K>
+int sort_instance(const int32_t *off_p, long long nseg, const K *keys_p, long long n, const Opts &opt);
+
+template <typename K>
 int run(Reader &in, const Opts &opt) {
+  if (in.binary()) {
+    BinaryHeader h;
+    std::memcpy(&h, in.data, sizeof(h));
+    if (h.version != 1 || h.key_bytes != sizeof(K)) die("binary instance does not match --type", nullptr);
+    if (h.nseg > static_cast<uint64_t>(INT32_MAX - 1) || h.n > (uint64_t{1} << 40))
+      die("bad binary header", nullptr);
+    const size_t off_at = sizeof(h), off_bytes = (h.nseg + 1) * 4;
+    const size_t keys_at = (off_at + off_bytes + 7) / 8 * 8;
+    if (keys_at + h.n * sizeof(K) > in.size) die("truncated binary instance", nullptr);
+    return sort_instance<K>(reinterpret_cast<const int32_t *>(in.data + off_at),
+                            static_cast<long long>(h.nseg),
+                            reinterpret_cast<const K *>(in.data + keys_at),
+                            static_cast<long long>(h.n), opt);
+  }
   const long long nseg = in.next_int();
   if (nseg < 0 || nseg > INT32_MAX - 1) die("bad segment count", nullptr);
   std::vector<int32_t> off(static_cast<size_t>(nseg) + 1);
@@ -140,6 +198,12 @@ int run(Reader &in, const Opts &opt) {
     if (!s) die("truncated key list", nullptr);
     k = parse_key<K>(s);
   }
+  return sort_instance<K>(off.data(), nseg, keys.data(), n, opt);
+}
+
+template <typename K>
+int sort_instance(const int32_t *off_p, long long nseg, const K *keys_p, long long n, const Opts &opt) {
+  const std::vector<int32_t> off(off_p, off_p + nseg + 1);
   std::vector<uint32_t> vals;
   if (opt.pairs) {
     vals.resize(static_cast<size_t>(n));
@@ -163,7 +227,7 @@ int run(Reader &in, const Opts &opt) {
   check_cuda(cudaEventCreate(&stop), "event");
 
   for (int e = 0; e < opt.execs; ++e) {
-    check_cuda(cudaMemcpyAsync(d_keys, keys.data(), kb, cudaMemcpyHostToDevice, stream), "copy keys");
+    check_cuda(cudaMemcpyAsync(d_keys, keys_p, kb, cudaMemcpyHostToDevice, stream), "copy keys");
     if (opt.pairs)
       check_cuda(cudaMemcpyAsync(d_vals, vals.data(), vb, cudaMemcpyHostToDevice, stream), "copy values");
     check_cuda(cudaEventRecord(start, stream), "record");
@@ -206,6 +270,7 @@ int run(Reader &in, const Opts &opt) {
 
 int main(int argc, char **argv) {
   Opts opt;
+  bool type_given = false;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     if (a == "--pairs") opt.pairs = true;
@@ -214,12 +279,24 @@ int main(int argc, char **argv) {
     else if (a == "--print") opt.timed = 0;
     else if (a == "--print-values") opt.print_values = true;
     else if (a == "--execs" && i + 1 < argc) opt.execs = std::atoi(argv[++i]);
-    else if (a == "--type" && i + 1 < argc) opt.type = argv[++i];
+    else if (a == "--type" && i + 1 < argc) {
+      opt.type = argv[++i];
+      type_given = true;
+    }
     else die("unknown option", a.c_str());
   }
   if (opt.execs < 1) opt.execs = 1;
   if (opt.heads && opt.type != "u32") die("--heads supports u32 keys only", nullptr);
   Reader in;
+  if (in.binary()) {  // the key type comes from the header
+    BinaryHeader h;
+    std::memcpy(&h, in.data, sizeof(h));
+    static const char *kinds4[] = {"u32", "i32", "f32"};
+    const std::string t = h.key_bytes == 8 ? "u64" : (h.key_kind < 3 ? kinds4[h.key_kind] : "?");
+    if (!type_given) opt.type = t;
+    else if (opt.type != t) die("--type does not match the binary instance", t.c_str());
+    if (opt.heads && opt.type != "u32") die("--heads supports u32 keys only", nullptr);
+  }
   if (opt.type == "u32") return run<uint32_t>(in, opt);
   if (opt.type == "i32") return run<int32_t>(in, opt);
   if (opt.type == "f32") return run<float>(in, opt);

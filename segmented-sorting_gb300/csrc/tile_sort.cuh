@@ -598,8 +598,20 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
   thread_sort<WT, KPT>(w);
 
   // ---- merge levels ---------------------------------------------------------------
+  // The level merging runs of KPT * 2^l words has work only where one of its
+  // run boundaries -- an odd multiple of KPT * 2^l, i.e. the first position of
+  // a thread t with ctz(t) = l -- falls inside a segment.  A chunk of several
+  // segments runs only the levels up to the highest such one (none at all
+  // when every thread's first position starts a segment).
+  int levels = 31;
+  if (multi) {
+    int need = -1;
+    if (tid > 0 && base < m && !((hb[base >> 5] >> (base & 31)) & 1u)) need = __ffs(tid) - 1;
+    levels = block_max<NT>(need, warp_s) + 1;
+  }
   bool dirty = true;  // W does not hold this thread's current words
-  for (int run = KPT; run < m; run <<= 1) {
+  int level = 0;
+  for (int run = KPT; run < m && level < levels; run <<= 1, ++level) {
     __syncthreads();  // previous readers of W are done
     if (dirty) {
 #pragma unroll

@@ -170,6 +170,39 @@ def batch_instance(spec: dict):
     return batch_offsets(spec), typed_keys(spec["n"], spec["seed"], spec["key_type"])
 
 
+# ---------------------------------------------------------------------------
+# Binary instance format (segsort_driver.exe reads it, gen_instance.exe
+# --binary writes it): 32-byte header {b"SGSB", version 1, key bytes (4/8),
+# key kind (0 unsigned, 1 signed, 2 float), nseg, n}, nseg+1 int32 offsets,
+# zero padding to a multiple of 8 bytes, n little-endian keys.
+_KIND = {np.dtype(np.uint32): (4, 0), np.dtype(np.int32): (4, 1),
+         np.dtype(np.float32): (4, 2), np.dtype(np.uint64): (8, 0)}
+
+
+def write_binary_instance(offsets: np.ndarray, keys: np.ndarray) -> bytes:
+    kb, kind = _KIND[keys.dtype]
+    head = np.array([1, kb, kind], dtype="<u4").tobytes()
+    counts = np.array([len(offsets) - 1, len(keys)], dtype="<u8").tobytes()
+    off = np.asarray(offsets, dtype="<i4").tobytes()
+    pad = b"\0" * ((8 - (32 + len(off)) % 8) % 8)
+    return b"SGSB" + head + counts + off + pad + keys.astype(keys.dtype.newbyteorder("<")).tobytes()
+
+
+def read_binary_instance(data: bytes):
+    """(offsets, keys) of a binary instance."""
+    if data[:4] != b"SGSB":
+        raise ValueError("not a binary instance")
+    version, kb, kind = np.frombuffer(data, dtype="<u4", count=3, offset=4)
+    nseg, n = (int(x) for x in np.frombuffer(data, dtype="<u8", count=2, offset=16))
+    if version != 1:
+        raise ValueError("unknown version")
+    off = np.frombuffer(data, dtype="<i4", count=nseg + 1, offset=32).astype(np.int32)
+    at = (32 + 4 * (nseg + 1) + 7) // 8 * 8
+    dt = {(4, 0): np.uint32, (4, 1): np.int32, (4, 2): np.float32, (8, 0): np.uint64}[(int(kb), int(kind))]
+    keys = np.frombuffer(data, dtype=np.dtype(dt).newbyteorder("<"), count=n, offset=at).astype(dt)
+    return off, keys
+
+
 def instance(workload: str, n: int, seed: int = 1, length: int = 0, nseg: int = 0,
              bits: int = 32):
     """(offsets, keys) of a named workload."""

@@ -152,3 +152,28 @@ def test_server_host_side_argument_checks(pkg):
     ws = L.segsort_batch_workspace_bytes(items, 2)
     assert ws > L.segsort_workspace_bytes(1 << 20, 4, 4, 4)
     assert L.segsort_batch_workspace_bytes(items, -1) == 0
+
+
+def test_extension_host_side_argument_checks(pkg):
+    """Descending, top-k and 64-bit-value entry points reject bad arguments
+    before any CUDA call, and return at once when there is nothing to sort."""
+    L = pkg.lib()
+    P = ctypes.c_void_p(16)
+    for t in pkg.KEY_TYPES:
+        f = getattr(L, f"segsort_pairs_{t}_desc")
+        assert f(None, None, 0, None, 0, None) == pkg.SEGSORT_OK
+        assert f(None, None, -1, None, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+        assert f(P, None, 10, P, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+        assert f(P, P, 1 << 30, P, 1, None) == pkg.SEGSORT_ERR_TOO_LARGE
+        g = getattr(L, f"segsort_pairs_{t}_v64")
+        assert g(None, None, 0, None, 0, None) == pkg.SEGSORT_OK
+        assert g(P, None, 10, P, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+        assert g(P, P, 1 << 30, P, 1, None) == pkg.SEGSORT_ERR_TOO_LARGE
+    assert L.segsort_keys_u32_desc(None, 10, P, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_keys_f32_desc(P, 10, None, 1, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    for t in ("u32", "f32"):
+        f = getattr(L, f"segsort_pairs_{t}_topk")
+        assert f(P, P, 10, P, 1, 0, 0, P, P, None, None) == pkg.SEGSORT_OK   # k = 0
+        assert f(P, P, 10, P, 1, -1, 0, P, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG
+        assert f(P, P, 10, P, 1, 4, 0, None, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG
+        assert f(P, None, 10, P, 1, 4, 0, P, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG

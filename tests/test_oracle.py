@@ -111,3 +111,27 @@ def test_planted_mistake_is_caught(oracle):
     k_bad = k.copy()
     k_bad[j], k_bad[j + 1] = k_bad[j + 1], k_bad[j]
     assert not np.array_equal(k_bad, g["ref_pair_keys"])
+
+
+def test_oracle_descending_and_64bit_values(oracle):
+    """The numpy restatement's descending mode against a plain Python stable
+    sort by decreasing key, with 64-bit values carried along."""
+    rng = np.random.default_rng(5)
+    for dt in (np.uint32, np.int32, np.float32, np.uint64):
+        n = 300
+        if dt == np.float32:
+            keys = rng.choice(np.array([-1.5, -0.0, 0.0, 2.0, 7.25], np.float32), n)
+        else:
+            keys = rng.integers(0, 6, n).astype(dt)
+        off = np.array([0, 7, 7, 100, 101, 250, 300], np.int32)
+        vals = rng.integers(0, 1 << 62, n, dtype=np.uint64)
+        k, v = oracle.segsort_numpy(keys, off, vals, descending=True)
+        ek, ev = keys.copy(), vals.copy()
+        bits = oracle.order_bits(keys)
+        for s in range(len(off) - 1):
+            idx = list(range(off[s], off[s + 1]))
+            idx = sorted(idx, key=lambda i: -int(bits[i]))  # stable
+            ek[off[s]:off[s + 1]] = keys[idx]
+            ev[off[s]:off[s + 1]] = vals[idx]
+        assert np.array_equal(k.view(np.uint8), ek.view(np.uint8)), dt
+        assert v.dtype == np.uint64 and np.array_equal(v, ev), dt
