@@ -286,6 +286,13 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
     rc = L.segsort_batch_plan_create(items, len(rows), ctypes.byref(plan))
     if rc != 0:
         raise pkg.SegsortError(rc, "segsort_batch_plan_create")
+    # Autotuner: the merge passes' launch shape for this batch, measured on
+    # its own data (no cache file: always measured here).
+    tuned = ctypes.c_int32()
+    restore()
+    rc = L.segsort_batch_plan_tune(plan, st, None, ctypes.byref(tuned))
+    if rc != 0:
+        raise pkg.SegsortError(rc, "segsort_batch_plan_tune")
 
     def replay():
         rc = L.segsort_batch_plan_launch(plan, st)
@@ -319,6 +326,7 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
         "speedup_plan_vs_plain": round(med["plain"] / med["plan"], 3),
         "plan_p99_ms": round(float(np.percentile(t_plan, 99)), 4),
         "identical_to_plain": identical, "plan_workspace_bytes": ws, "steps": steps,
+        "tuned_merge_ctas_per_sm": tuned.value,
         "launches": {"plain": 3 * len(specs), "plan_graph": 3 * len(types)},
     }
 

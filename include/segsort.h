@@ -222,6 +222,21 @@ int segsort_pairs_u64_v64(uint64_t *d_keys, uint64_t *d_vals, int64_t n,
                           segsort_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Segmented reduce-by-key (no reference counterpart; the step after the sort
+ * in typical pipelines).  Sorts every segment ascending in place, then, for
+ * every run of equal keys inside a segment, in segment order: its key in
+ * d_out_keys, the sum of its values (64-bit, no overflow) in d_out_sums and
+ * its length in d_out_counts; d_out_offsets[s] (nseg + 1 entries) is the
+ * index of segment s's first run, d_out_offsets[nseg] the number of runs.
+ * The three run arrays need room for n runs.
+ * ---------------------------------------------------------------------- */
+int segsort_pairs_u32_reduce_by_key(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                                    const int32_t *d_offsets, int32_t nseg,
+                                    uint32_t *d_out_keys, uint64_t *d_out_sums,
+                                    uint32_t *d_out_counts, int32_t *d_out_offsets,
+                                    segsort_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Batched form: many independent instances, each with its own keys, uint32
  * values and offsets, sorted by one launch of each kernel per key type
  * instead of one sequence of launches per instance.  No counterpart in the
@@ -266,6 +281,16 @@ typedef struct segsort_batch_plan_s *segsort_batch_plan;
 int segsort_batch_plan_create(const segsort_batch_item *items, int32_t count,
                               segsort_batch_plan *plan);
 int segsort_batch_plan_launch(segsort_batch_plan plan, segsort_stream_t stream);
+/* Autotuner: picks the launch shape of the plan's merge passes (1, 2 or 3
+ * resident CTAs per SM) by replaying the plan four times per shape on
+ * `stream` (the items' buffers are sorted by it, as by a launch) and keeping
+ * the fastest.  With cache_path given, the choice is looked up first in, and
+ * after a measurement appended to, that text file, keyed by the class of the
+ * batch (key types present; log2 of the total keys, the largest item and the
+ * key-weighted mean segment length).  *ctas_per_sm (optional) receives the
+ * choice.  Untuned plans use 3. */
+int segsort_batch_plan_tune(segsort_batch_plan plan, segsort_stream_t stream,
+                            const char *cache_path, int32_t *ctas_per_sm);
 size_t segsort_batch_plan_workspace_bytes(segsort_batch_plan plan);
 void segsort_batch_plan_destroy(segsort_batch_plan plan);
 

@@ -68,9 +68,11 @@ SIGNATURES = {
     **{f"segsort_pairs_{t}_topk": ([_P, _P, _I64, _P, _I32, _I64, ctypes.c_int, _P, _P, _P, _P],
                                    ctypes.c_int) for t in ("u32", "f32")},
     **{f"segsort_pairs_{t}_v64": ([_P, _P, _I64, _P, _I32, _P], ctypes.c_int) for t in KEY_TYPES},
+    "segsort_pairs_u32_reduce_by_key": ([_P, _P, _I64, _P, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "segsort_pairs_batch": ([ctypes.POINTER(BatchItem), _I32, _P], ctypes.c_int),
     "segsort_batch_plan_create": ([ctypes.POINTER(BatchItem), _I32, ctypes.POINTER(_P)], ctypes.c_int),
     "segsort_batch_plan_launch": ([_P, _P], ctypes.c_int),
+    "segsort_batch_plan_tune": ([_P, _P, ctypes.c_char_p, ctypes.POINTER(_I32)], ctypes.c_int),
     "segsort_batch_plan_workspace_bytes": ([_P], ctypes.c_size_t),
     "segsort_batch_plan_destroy": ([_P], None),
     "segsort_batch_workspace_bytes": ([ctypes.POINTER(BatchItem), _I32], ctypes.c_size_t),
@@ -255,6 +257,15 @@ class BatchPlan:
 
     def launch(self, stream=None) -> None:
         _check(lib().segsort_batch_plan_launch(self._h, _stream_ptr(stream)), "segsort_batch_plan_launch")
+
+    def tune(self, cache_path: str | None = None, stream=None) -> int:
+        """Choose the merge passes' launch shape (see segsort_batch_plan_tune);
+        returns the chosen CTAs per SM."""
+        k = ctypes.c_int32()
+        path = None if cache_path is None else str(cache_path).encode()
+        _check(lib().segsort_batch_plan_tune(self._h, _stream_ptr(stream), path, ctypes.byref(k)),
+               "segsort_batch_plan_tune")
+        return k.value
 
     @property
     def workspace_bytes(self) -> int:

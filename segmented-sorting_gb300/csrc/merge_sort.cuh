@@ -385,6 +385,27 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
           }
           if (tid == 0 && more) publish(c ^ 1);
           __syncthreads();
+          // Start moving the next item's windows into L2 while this one is
+          // stored.
+          if (more && (slot_m[c ^ 1].y & 2)) {
+            const int4 nd2 = slot_d[c ^ 1], nm2 = slot_m[c ^ 1];
+            const int64_t nla = nd2.y, nlb = nd2.z, nd0 = nd2.w;
+            const int64_t nd1 = min(nd0 + T, nla + nlb);
+            const int64_t ns0 = slot_s0[c ^ 1];
+            const int64_t ns1 = nd1 == nla + nlb ? nla : static_cast<int64_t>(slot_s1[c ^ 1]);
+            if (ns1 >= ns0 && nd1 - nd0 >= ns1 - ns0) {
+              const SideBuffers<K> NB = sp(nm2.x);
+              const bool nt = (nm2.y & 1) != 0;
+              const K *nk = (nt ? NB.tmp_keys : NB.keys) + nd2.x;
+              prefetch_l2<NT>(nk + ns0, ns1 - ns0);
+              prefetch_l2<NT>(nk + nla + (nd0 - ns0), (nd1 - nd0) - (ns1 - ns0));
+              if constexpr (PAIRS) {
+                const uint32_t *nv = (nt ? NB.tmp_vals : NB.vals) + nd2.x;
+                prefetch_l2<NT>(nv + ns0, ns1 - ns0);
+                prefetch_l2<NT>(nv + nla + (nd0 - ns0), (nd1 - nd0) - (ns1 - ns0));
+              }
+            }
+          }
           store_range<NT>(dk, m, [&](int x) { return Ok[MS::oslot(x)]; });
           if constexpr (PAIRS) store_range<NT>(dv, m, [&](int x) { return Ov[MS::oslot(x)]; });
           continue;

@@ -10,13 +10,18 @@
 // sequence of launches and grid barriers each.
 //
 // A plan fixes the items, allocates one buffer for every group's table and
-// workspace, and captures the launches into a CUDA graph; a launch replays
-// the graph.
+// workspace, and captures the launches into CUDA graphs, one per launch
+// shape of the merge passes; a launch replays the chosen graph.  The tuner
+// measures the shapes on the plan's own data and caches the fastest per
+// class of batch (key types, sizes and mean segment length) in a file.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -155,7 +160,7 @@ struct BatchKernels {
   }
 
   static int enqueue(const Group &G, unsigned char *buf, const DeviceState &S, int dev,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int merge_per_sm) {
     const BatchInst *tab = reinterpret_cast<const BatchInst *>(buf + G.tab_off);
     const int32_t count = static_cast<int32_t>(G.insts.size());
     const LargeWs<K> W = ws_views<K, true>(buf + G.ws_off, G.L);
@@ -172,8 +177,9 @@ struct BatchKernels {
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     const int64_t items = G.total_n / MergeShape<K>::T + 1;
+    const int per_sm = merge_per_sm > 0 ? std::min(merge_per_sm, mo) : mo;
     const unsigned grid =
-        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(mo) * S.sms, items));
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(per_sm) * S.sms, items));
     BatchSpace<K> sp{tab, W.tmp_keys, W.tmp_vals};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -200,12 +206,12 @@ cudaError_t prepare_group(const Group &G, int dev) {
 }
 
 int enqueue_group(const Group &G, unsigned char *buf, const DeviceState &S, int dev,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, int merge_per_sm) {
   switch (G.key_type) {
-    case SEGSORT_KEY_U32: return BatchKernels<uint32_t>::enqueue(G, buf, S, dev, stream);
-    case SEGSORT_KEY_I32: return BatchKernels<int32_t>::enqueue(G, buf, S, dev, stream);
-    case SEGSORT_KEY_F32: return BatchKernels<float>::enqueue(G, buf, S, dev, stream);
-    default: return BatchKernels<uint64_t>::enqueue(G, buf, S, dev, stream);
+    case SEGSORT_KEY_U32: return BatchKernels<uint32_t>::enqueue(G, buf, S, dev, stream, merge_per_sm);
+    case SEGSORT_KEY_I32: return BatchKernels<int32_t>::enqueue(G, buf, S, dev, stream, merge_per_sm);
+    case SEGSORT_KEY_F32: return BatchKernels<float>::enqueue(G, buf, S, dev, stream, merge_per_sm);
+    default: return BatchKernels<uint64_t>::enqueue(G, buf, S, dev, stream, merge_per_sm);
   }
 }
 
@@ -215,13 +221,36 @@ int prepare_all(const BatchLayout &B, int dev) {
   return SEGSORT_OK;
 }
 
+// merge_per_sm: resident merge-pass CTAs per SM (0: as many as fit).
 int enqueue_all(const BatchLayout &B, unsigned char *buf, const DeviceState &S, int dev,
-                cudaStream_t stream) {
+                cudaStream_t stream, int merge_per_sm = 0) {
   for (const Group &G : B.groups) {
-    const int rc = enqueue_group(G, buf, S, dev, stream);
+    const int rc = enqueue_group(G, buf, S, dev, stream, merge_per_sm);
     if (rc != SEGSORT_OK) return rc;
   }
   return SEGSORT_OK;
+}
+
+// Class of a batch for the autotuner's cache: the key types present and the
+// log2 buckets of the total keys, the largest item and the key-weighted mean
+// segment length (n / nseg of each item, known on the host).
+std::string batch_class(const segsort_batch_item *items, int32_t count) {
+  int64_t total = 0, largest = 0;
+  double weighted = 0.0;
+  unsigned types = 0;
+  for (int32_t i = 0; i < count; ++i) {
+    const segsort_batch_item &it = items[i];
+    if (it.n <= 0 || it.nseg <= 0) continue;
+    total += it.n;
+    largest = std::max<int64_t>(largest, it.n);
+    weighted += static_cast<double>(it.n) * (static_cast<double>(it.n) / it.nseg);
+    types |= 1u << it.key_type;
+  }
+  auto lg = [](double x) { return x >= 1.0 ? static_cast<int>(std::floor(std::log2(x))) : 0; };
+  char buf[96];
+  std::snprintf(buf, sizeof(buf), "t%u-n%d-max%d-len%d", types, lg(static_cast<double>(total)),
+                lg(static_cast<double>(largest)), lg(total > 0 ? weighted / total : 0.0));
+  return buf;
 }
 
 int current_device(int *dev, DeviceState **S) {
@@ -244,12 +273,19 @@ cudaError_t batch_device_status(bool clear, uint32_t *value) {
 
 }  // namespace segsort
 
+// A plan holds one captured graph per launch shape of the merge passes (1, 2
+// or 3 resident CTAs per SM); `choice` is the one launches replay.
+constexpr int kPlanShapes = 3;
+
 struct segsort_batch_plan_s {
   int dev = 0;
   void *buf = nullptr;
   size_t bytes = 0;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph[kPlanShapes] = {};
+  cudaGraphExec_t exec[kPlanShapes] = {};
+  int choice = kPlanShapes - 1;
+  bool empty = false;
+  std::string cls;
 };
 
 extern "C" {
@@ -317,18 +353,25 @@ int segsort_batch_plan_create(const segsort_batch_item *items, int32_t count,
       }
     }
     if (rc != SEGSORT_OK) break;
-    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    P->empty = B.groups.empty();
+    P->cls = batch_class(items, count);
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
       rc = SEGSORT_ERR_CUDA;
       break;
     }
-    rc = enqueue_all(B, buf, *S, dev, cs);
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
-    if (rc == SEGSORT_OK && ce != cudaSuccess) rc = SEGSORT_ERR_CUDA;
-    P->graph = graph;
-    if (rc != SEGSORT_OK) break;
-    if (cudaGraphInstantiate(&P->exec, P->graph, 0) != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+    for (int k = 0; k < kPlanShapes && rc == SEGSORT_OK; ++k) {
+      if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      rc = enqueue_all(B, buf, *S, dev, cs, k + 1);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+      if (rc == SEGSORT_OK && ce != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+      P->graph[k] = graph;
+      if (rc == SEGSORT_OK && cudaGraphInstantiate(&P->exec[k], P->graph[k], 0) != cudaSuccess)
+        rc = SEGSORT_ERR_CUDA;
+    }
   } while (false);
   if (cs != nullptr) cudaStreamDestroy(cs);
   if (rc != SEGSORT_OK) {
@@ -342,12 +385,77 @@ int segsort_batch_plan_create(const segsort_batch_item *items, int32_t count,
 
 int segsort_batch_plan_launch(segsort_batch_plan plan, segsort_stream_t s) {
   if (plan == nullptr) return SEGSORT_ERR_INVALID_ARG;
-  if (plan->exec == nullptr) return SEGSORT_OK;  // nothing to sort
+  if (plan->empty) return SEGSORT_OK;  // nothing to sort
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev != plan->dev) return SEGSORT_ERR_INVALID_ARG;
-  return cudaGraphLaunch(plan->exec, reinterpret_cast<cudaStream_t>(s)) == cudaSuccess
+  return cudaGraphLaunch(plan->exec[plan->choice], reinterpret_cast<cudaStream_t>(s)) ==
+                 cudaSuccess
              ? SEGSORT_OK
              : SEGSORT_ERR_CUDA;
+}
+
+int segsort_batch_plan_tune(segsort_batch_plan plan, segsort_stream_t s, const char *cache_path,
+                            int32_t *ctas_per_sm) {
+  if (plan == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  auto done = [&](int rc) {
+    if (ctas_per_sm) *ctas_per_sm = plan->choice + 1;
+    return rc;
+  };
+  if (plan->empty) return done(SEGSORT_OK);
+  // A cached choice for this class of batch.
+  if (cache_path != nullptr) {
+    if (FILE *f = std::fopen(cache_path, "r")) {
+      char cls[128];
+      int k = 0;
+      bool found = false;
+      while (std::fscanf(f, "%127s %d", cls, &k) == 2) {
+        if (plan->cls == cls && k >= 1 && k <= kPlanShapes) {
+          plan->choice = k - 1;
+          found = true;
+        }
+      }
+      std::fclose(f);
+      if (found) return done(SEGSORT_OK);
+    }
+  }
+  // Measure every shape: one warm-up replay, then the median of three.
+  const cudaStream_t stream = reinterpret_cast<cudaStream_t>(s);
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    if (a) cudaEventDestroy(a);
+    return SEGSORT_ERR_CUDA;
+  }
+  int rc = SEGSORT_OK;
+  float best = 0.f;
+  int best_k = plan->choice;
+  for (int k = 0; k < kPlanShapes && rc == SEGSORT_OK; ++k) {
+    float t[3];
+    for (int r = -1; r < 3 && rc == SEGSORT_OK; ++r) {
+      if (cudaEventRecord(a, stream) != cudaSuccess || cudaGraphLaunch(plan->exec[k], stream) != cudaSuccess ||
+          cudaEventRecord(b, stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      if (r >= 0) cudaEventElapsedTime(&t[r], a, b);
+    }
+    if (rc != SEGSORT_OK) break;
+    std::sort(t, t + 3);
+    if (k == 0 || t[1] < best) {
+      best = t[1];
+      best_k = k;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc != SEGSORT_OK) return done(rc);
+  plan->choice = best_k;
+  if (cache_path != nullptr) {
+    if (FILE *f = std::fopen(cache_path, "a")) {
+      std::fprintf(f, "%s %d\n", plan->cls.c_str(), best_k + 1);
+      std::fclose(f);
+    }
+  }
+  return done(SEGSORT_OK);
 }
 
 size_t segsort_batch_plan_workspace_bytes(segsort_batch_plan plan) {
@@ -356,8 +464,10 @@ size_t segsort_batch_plan_workspace_bytes(segsort_batch_plan plan) {
 
 void segsort_batch_plan_destroy(segsort_batch_plan plan) {
   if (plan == nullptr) return;
-  if (plan->exec) cudaGraphExecDestroy(plan->exec);
-  if (plan->graph) cudaGraphDestroy(plan->graph);
+  for (int k = 0; k < kPlanShapes; ++k) {
+    if (plan->exec[k]) cudaGraphExecDestroy(plan->exec[k]);
+    if (plan->graph[k]) cudaGraphDestroy(plan->graph[k]);
+  }
   if (plan->buf) cudaFree(plan->buf);
   delete plan;
 }

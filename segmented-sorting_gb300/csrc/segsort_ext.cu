@@ -175,6 +175,228 @@ int v64_impl(K *keys, uint64_t *vals, int64_t n, const int32_t *off, int32_t nse
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Segmented reduce-by-key after the sort.  Positions are handled in 32-bit
+// words of a bitmap: segbits marks segment starts, headbits marks run heads
+// (a segment start, or a key different from the previous key), and the run
+// of a head at position p is the number of heads before p, read from an
+// exclusive prefix of the per-word head counts plus a popcount.
+constexpr int kScanItems = 1024;  // words per block of the word-count scan
+
+__global__ void __launch_bounds__(kEwThreads) mark_starts_kernel(Offsets off, uint32_t *segbits) {
+  const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= off.nseg) return;
+  const int64_t b = off(s), e = off(s + 1);
+  if (e > b) atomicOr(&segbits[b >> 5], 1u << (b & 31));
+}
+
+// Covered positions [lo, hi) = [off(0), off(nseg)), written to the device
+// (the offsets live there).
+__global__ void lohi_kernel(Offsets off, uint32_t *lohi) {
+  lohi[0] = static_cast<uint32_t>(off(0));
+  lohi[1] = static_cast<uint32_t>(off(off.nseg));
+}
+
+// One thread per word: head bits and their count.
+__global__ void __launch_bounds__(kEwThreads)
+head_bits_kernel(const uint32_t *keys, const uint32_t *segbits, const uint32_t *lohi,
+                 int64_t words, uint32_t *headbits, uint32_t *wcount) {
+  const int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= words) return;
+  const int64_t lo = lohi[0], hi = lohi[1];
+  const uint32_t sb = segbits[w];
+  uint32_t bits = 0;
+  const int64_t p0 = w * 32;
+  uint32_t prev = p0 > 0 && p0 - 1 >= lo && p0 - 1 < hi ? keys[p0 - 1] : 0u;
+  for (int j = 0; j < 32; ++j) {
+    const int64_t p = p0 + j;
+    if (p >= hi) break;
+    if (p < lo) continue;
+    const uint32_t k = keys[p];
+    if (((sb >> j) & 1u) || p == lo || k != prev) bits |= 1u << j;
+    prev = k;
+  }
+  headbits[w] = bits;
+  wcount[w] = static_cast<uint32_t>(__popc(bits));
+}
+
+// Exclusive scan of wcount in blocks of kScanItems words: per-block totals,
+// then (one CTA) their exclusive prefix and the grand total, then the
+// per-word prefix.  Counts fit uint32 (n < 2^30).
+__global__ void __launch_bounds__(kEwThreads)
+block_totals_kernel(const uint32_t *wcount, int64_t words, uint32_t *btotal) {
+  __shared__ int warp_s[kEwThreads / 32];
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanItems;
+  uint32_t sum = 0;
+  for (int i = threadIdx.x; i < kScanItems; i += kEwThreads)
+    if (base + i < words) sum += wcount[base + i];
+  uint32_t tot;
+  block_exclusive_add<kEwThreads>(sum, tot, warp_s);
+  if (threadIdx.x == 0) btotal[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kEwThreads)
+scan_totals_kernel(uint32_t *btotal, int64_t nb, uint32_t *grand) {
+  __shared__ int warp_s[kEwThreads / 32];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t b0 = 0; b0 < nb; b0 += kEwThreads) {
+    const int64_t b = b0 + threadIdx.x;
+    const uint32_t v = b < nb ? btotal[b] : 0u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_add<kEwThreads>(v, tot, warp_s);
+    if (b < nb) btotal[b] = carry + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *grand = carry;
+}
+
+__global__ void __launch_bounds__(kEwThreads)
+word_prefix_kernel(const uint32_t *wcount, int64_t words, const uint32_t *bprefix,
+                   uint32_t *wprefix) {
+  __shared__ int warp_s[kEwThreads / 32];
+  __shared__ uint32_t carry;
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanItems;
+  if (threadIdx.x == 0) carry = bprefix[blockIdx.x];
+  __syncthreads();
+  for (int i0 = 0; i0 < kScanItems; i0 += kEwThreads) {
+    const int64_t w = base + i0 + threadIdx.x;
+    const uint32_t v = w < words ? wcount[w] : 0u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_add<kEwThreads>(v, tot, warp_s);
+    if (w < words) wprefix[w] = carry + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kEwThreads)
+zero_runs_kernel(uint64_t *sums, uint32_t *counts, const uint32_t *grand) {
+  const int64_t runs = *grand;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < runs;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    sums[r] = 0;
+    counts[r] = 0;
+  }
+}
+
+// One thread per word: keys of its heads, and its elements' values and
+// counts added to their runs (one atomic per run piece of the word).
+__global__ void __launch_bounds__(kEwThreads)
+run_write_kernel(const uint32_t *keys, const uint32_t *vals, const uint32_t *headbits,
+                 const uint32_t *wprefix, const uint32_t *lohi, int64_t words,
+                 uint32_t *out_keys, uint64_t *out_sums, uint32_t *out_counts) {
+  const int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= words) return;
+  const int64_t lo = lohi[0], hi = lohi[1];
+  const uint32_t hb = headbits[w];
+  const int64_t p0 = w * 32;
+  // Run of the first covered position of the word: the heads before it.
+  int64_t r = static_cast<int64_t>(wprefix[w]) - 1;
+  uint64_t sum = 0;
+  uint32_t cnt = 0;
+  for (int j = 0; j < 32; ++j) {
+    const int64_t p = p0 + j;
+    if (p >= hi) break;
+    if (p < lo) continue;
+    if ((hb >> j) & 1u) {
+      if (cnt) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(&out_sums[r]), sum);
+        atomicAdd(&out_counts[r], cnt);
+      }
+      ++r;
+      out_keys[r] = keys[p];
+      sum = 0;
+      cnt = 0;
+    }
+    sum += vals[p];
+    ++cnt;
+  }
+  if (cnt && r >= 0) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(&out_sums[r]), sum);
+    atomicAdd(&out_counts[r], cnt);
+  }
+}
+
+// out_offsets[s]: run index of segment s's first element (the number of
+// heads before it); the total number of runs for s = nseg and for segments
+// that start at or after the covered end.
+__global__ void __launch_bounds__(kEwThreads)
+run_offsets_kernel(Offsets off, const uint32_t *headbits, const uint32_t *wprefix,
+                   const uint32_t *lohi, const uint32_t *grand, int32_t *out_offsets) {
+  const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s > off.nseg) return;
+  const int64_t hi = lohi[1];
+  const int64_t p = off(s);
+  uint32_t r = *grand;
+  if (s < off.nseg && p < hi) {
+    const int64_t w = p >> 5;
+    const uint32_t below = (1u << (p & 31)) - 1u;
+    r = wprefix[w] + static_cast<uint32_t>(__popc(headbits[w] & below));
+  }
+  out_offsets[s] = static_cast<int32_t>(r);
+}
+
+int reduce_by_key_impl(uint32_t *keys, uint32_t *vals, int64_t n, const int32_t *off, int32_t nseg,
+                       uint32_t *out_keys, uint64_t *out_sums, uint32_t *out_counts,
+                       int32_t *out_offsets, cudaStream_t s) {
+  if (n < 0 || nseg < 0) return SEGSORT_ERR_INVALID_ARG;
+  if (nseg > 0 && (off == nullptr || out_offsets == nullptr)) return SEGSORT_ERR_INVALID_ARG;
+  if (n > 0 && nseg > 0 &&
+      (keys == nullptr || vals == nullptr || out_keys == nullptr || out_sums == nullptr ||
+       out_counts == nullptr))
+    return SEGSORT_ERR_INVALID_ARG;
+  if (n >= (int64_t{1} << 30)) return SEGSORT_ERR_TOO_LARGE;
+  if (nseg == 0) return SEGSORT_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  DeviceState *S = device_state(dev);
+  cudaMemPool_t pool = S ? device_pool(*S, dev) : nullptr;
+  const int64_t words = (n + 31) / 32 + 1;
+  const int64_t nb = (words + kScanItems - 1) / kScanItems;
+  const size_t wbytes = align256(static_cast<size_t>(words) * 4);
+  const size_t total = 4 * wbytes + align256(static_cast<size_t>(nb) * 4) + 256;
+  unsigned char *ws = nullptr;
+  if (pool == nullptr ||
+      cudaMallocFromPoolAsync(reinterpret_cast<void **>(&ws), total, pool, s) != cudaSuccess) {
+    cudaGetLastError();
+    return SEGSORT_ERR_NO_MEMORY;
+  }
+  uint32_t *segbits = reinterpret_cast<uint32_t *>(ws);
+  uint32_t *headbits = reinterpret_cast<uint32_t *>(ws + wbytes);
+  uint32_t *wcount = reinterpret_cast<uint32_t *>(ws + 2 * wbytes);
+  uint32_t *wprefix = reinterpret_cast<uint32_t *>(ws + 3 * wbytes);
+  uint32_t *btotal = reinterpret_cast<uint32_t *>(ws + 4 * wbytes);
+  uint32_t *grand = reinterpret_cast<uint32_t *>(ws + 4 * wbytes + align256(static_cast<size_t>(nb) * 4));
+  uint32_t *lohi = grand + 1;
+  int rc = n > 0 ? sort_typed<uint32_t>(keys, vals, n, off, nseg, s) : SEGSORT_OK;
+  const Offsets o{off, nseg, 0, n};
+  if (rc == SEGSORT_OK) {
+    lohi_kernel<<<1, 1, 0, s>>>(o, lohi);
+    if (cudaMemsetAsync(segbits, 0, wbytes, s) != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+  }
+  if (rc == SEGSORT_OK) {
+    mark_starts_kernel<<<ew_blocks(nseg), kEwThreads, 0, s>>>(o, segbits);
+    head_bits_kernel<<<ew_blocks(words), kEwThreads, 0, s>>>(keys, segbits, lohi, words, headbits,
+                                                            wcount);
+    block_totals_kernel<<<static_cast<unsigned>(nb), kEwThreads, 0, s>>>(wcount, words, btotal);
+    scan_totals_kernel<<<1, kEwThreads, 0, s>>>(btotal, nb, grand);
+    word_prefix_kernel<<<static_cast<unsigned>(nb), kEwThreads, 0, s>>>(wcount, words, btotal, wprefix);
+    zero_runs_kernel<<<static_cast<unsigned>(S->sms * 4), kEwThreads, 0, s>>>(out_sums, out_counts, grand);
+    run_write_kernel<<<ew_blocks(words), kEwThreads, 0, s>>>(keys, vals, headbits, wprefix, lohi,
+                                                            words, out_keys, out_sums, out_counts);
+    run_offsets_kernel<<<ew_blocks(static_cast<int64_t>(nseg) + 1), kEwThreads, 0, s>>>(
+        o, headbits, wprefix, lohi, grand, out_offsets);
+    if (cudaGetLastError() != cudaSuccess) rc = SEGSORT_ERR_CUDA;
+  }
+  if (cudaFreeAsync(ws, s) != cudaSuccess && rc == SEGSORT_OK) rc = SEGSORT_ERR_CUDA;
+  return rc;
+}
+
 }  // namespace
 }  // namespace segsort
 
@@ -238,3 +460,11 @@ int segsort_pairs_u64_v64(uint64_t *k, uint64_t *v, int64_t n, const int32_t *o,
 }
 
 }  // extern "C"
+
+extern "C" int segsort_pairs_u32_reduce_by_key(uint32_t *k, uint32_t *v, int64_t n, const int32_t *o,
+                                               int32_t ns, uint32_t *ok, uint64_t *sums,
+                                               uint32_t *counts, int32_t *out_off,
+                                               segsort_stream_t s) {
+  return segsort::reduce_by_key_impl(k, v, n, o, ns, ok, sums, counts, out_off,
+                                     reinterpret_cast<cudaStream_t>(s));
+}

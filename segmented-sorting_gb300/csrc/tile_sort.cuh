@@ -272,6 +272,16 @@ __device__ __forceinline__ void store_range(T *__restrict__ dst, int m, G &&g) {
   if (tail0 + tid < m) __stcs(dst + tail0 + tid, g(tail0 + tid));
 }
 
+// Asks L2 for the elements [0, count) of p: one prefetch per 128-byte line,
+// spread over the CTA's threads.  A hint for data a later CTA or item reads.
+template <int NT, typename T>
+__device__ __forceinline__ void prefetch_l2(const T *p, int64_t count) {
+  const char *b = reinterpret_cast<const char *>(p);
+  const int64_t bytes = count * static_cast<int64_t>(sizeof(T));
+  for (int64_t o = static_cast<int64_t>(threadIdx.x) * 128; o < bytes; o += NT * 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(b + o));
+}
+
 // Exclusive running maximum over the threads of the CTA (-1 for thread 0).
 template <int NT>
 __device__ __forceinline__ int block_exclusive_max(int v, int *warp_s) {

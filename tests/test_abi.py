@@ -177,3 +177,21 @@ def test_extension_host_side_argument_checks(pkg):
         assert f(P, P, 10, P, 1, -1, 0, P, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG
         assert f(P, P, 10, P, 1, 4, 0, None, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG
         assert f(P, None, 10, P, 1, 4, 0, P, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG
+
+
+def test_reduce_by_key_host_side_argument_checks(pkg):
+    L = pkg.lib()
+    P = ctypes.c_void_p(16)
+    f = L.segsort_pairs_u32_reduce_by_key
+    assert f(None, None, 0, None, 0, None, None, None, None, None) == pkg.SEGSORT_OK
+    assert f(P, P, -1, P, 1, P, P, P, P, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert f(P, P, 10, P, 1, P, P, P, None, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert f(P, None, 10, P, 1, P, P, P, P, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert f(P, P, 10, P, 1, P, None, P, P, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert f(P, P, 1 << 30, P, 1, P, P, P, P, None) == pkg.SEGSORT_ERR_TOO_LARGE
+
+
+def test_batch_tune_rejects_a_missing_plan(pkg):
+    L = pkg.lib()
+    k = ctypes.c_int32()
+    assert L.segsort_batch_plan_tune(None, None, None, ctypes.byref(k)) == pkg.SEGSORT_ERR_INVALID_ARG

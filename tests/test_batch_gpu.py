@@ -199,3 +199,40 @@ def test_batch_mixed_64_instances_match_plain_calls(pkg, cuda, inst):
         assert np.array_equal(k.view(np.uint8), pk.view(np.uint8)), (d.key_type, d.n)
         assert np.array_equal(v, pv), (d.key_type, d.n)
         del d.kbuf, d.vbuf
+
+
+def test_batch_plan_tuner_caches_its_choice(pkg, cuda, inst, oracle, tmp_path):
+    """The tuner measures the launch shapes, records the choice for the
+    batch's class in the cache file, and a second plan of the same class
+    takes it from the file; results stay exact."""
+    torch = cuda
+    cases = _mix(inst)[::2]
+    dev = [_DevInstance(torch, k, np.arange(len(k), dtype=np.uint32), o, t, h) for k, o, t, h in cases]
+    items = (pkg.BatchItem * len(dev))(*[d.item(pkg) for d in dev])
+    L = pkg.lib()
+    cache = tmp_path / "tune.txt"
+    st = torch.cuda.current_stream().cuda_stream
+    chosen = []
+    for rep in range(2):
+        plan = ctypes.c_void_p()
+        assert L.segsort_batch_plan_create(items, len(dev), ctypes.byref(plan)) == pkg.SEGSORT_OK
+        try:
+            k = ctypes.c_int32()
+            assert L.segsort_batch_plan_tune(plan, st, str(cache).encode(), ctypes.byref(k)) == 0
+            assert 1 <= k.value <= 3
+            chosen.append(k.value)
+            for d in dev:
+                d.reset(torch)
+            assert L.segsort_batch_plan_launch(plan, st) == pkg.SEGSORT_OK
+            torch.cuda.synchronize()
+            assert pkg.device_status() == pkg.SEGSORT_OK
+            for d in dev:
+                kk, vv = d.result()
+                ek, ev = _oracle_of(oracle, d.keys, d.off, d.heads)
+                assert np.array_equal(kk.view(np.uint8), ek.view(np.uint8))
+                assert np.array_equal(vv, ev)
+        finally:
+            L.segsort_batch_plan_destroy(plan)
+    lines = cache.read_text().split("\n")
+    assert len([ln for ln in lines if ln.strip()]) == 1  # measured once, then read back
+    assert chosen[0] == chosen[1] == int(lines[0].split()[1])

@@ -1,7 +1,8 @@
-"""GPU parity of the extensions: stable descending order, segmented top-k and
-64-bit values, through the C ABI, bit for bit against the oracle (numpy
-restatement with descending=True / 64-bit values), with guard bands around
-every buffer."""
+"""GPU parity of the extensions: stable descending order, segmented top-k,
+64-bit values and segmented reduce-by-key, through the C ABI, bit for bit
+against the oracle (numpy restatement with descending=True / 64-bit values,
+and a Python loop over the oracle's sorted runs), with guard bands around
+the buffers of the in-place forms."""
 from __future__ import annotations
 
 import numpy as np
@@ -154,3 +155,58 @@ def test_64bit_values_match_oracle(pkg, cuda, inst, oracle):
         ek, ev = oracle.segsort_numpy(keys, off, vals)
         assert np.array_equal(k.view(np.uint8), ek.view(np.uint8)), (keys.dtype, n)
         assert np.array_equal(v, ev), (keys.dtype, n)
+
+
+def _reduce_oracle(oracle, keys, off, vals):
+    k, v = oracle.segsort_numpy(keys, off, vals)
+    ok, osum, ocnt, ooff = [], [], [], []
+    for s in range(len(off) - 1):
+        ooff.append(len(ok))
+        b, e = int(off[s]), int(off[s + 1])
+        i = b
+        while i < e:
+            j = i
+            while j < e and k[j] == k[i]:
+                j += 1
+            ok.append(k[i])
+            osum.append(int(v[i:j].astype(np.uint64).sum()))
+            ocnt.append(j - i)
+            i = j
+    ooff.append(len(ok))
+    return (np.array(ok, np.uint32), np.array(osum, np.uint64), np.array(ocnt, np.uint32),
+            np.array(ooff, np.int32), k)
+
+
+def test_reduce_by_key_matches_oracle(pkg, cuda, inst, oracle):
+    torch = cuda
+    L = pkg.lib()
+    rng = np.random.default_rng(3)
+    cases = [
+        (inst.uniform_keys(50000, 5, bits=6), inst.lognormal_offsets(50000, 6, empty_frac=0.05)),
+        (inst.uniform_keys(20000, 7, bits=32), inst.equal_offsets_ragged(20000, 333)),
+        (inst.uniform_keys(9000, 8, bits=1), np.array([5, 5, 100, 8000, 8000, 8990], np.int32)),
+        (np.zeros(4096 * 3, np.uint32), np.array([0, 4096 * 3], np.int32)),
+    ]
+    for keys, off in cases:
+        n = len(keys)
+        vals = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+        dk = torch.from_numpy(keys.view(np.int32).copy()).cuda()
+        dv = torch.from_numpy(vals.view(np.int32).copy()).cuda()
+        do = torch.from_numpy(off).cuda()
+        nseg = len(off) - 1
+        ok = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+        osum = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+        ocnt = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+        ooff = torch.full((nseg + 1,), -1, dtype=torch.int32, device="cuda")
+        rc = L.segsort_pairs_u32_reduce_by_key(dk.data_ptr(), dv.data_ptr(), n, do.data_ptr(), nseg,
+                                               ok.data_ptr(), osum.data_ptr(), ocnt.data_ptr(),
+                                               ooff.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        assert rc == pkg.SEGSORT_OK
+        torch.cuda.synchronize()
+        ek, es, ec, eo, sorted_keys = _reduce_oracle(oracle, keys, off, vals)
+        runs = int(eo[-1])
+        assert np.array_equal(ooff.cpu().numpy(), eo)
+        assert np.array_equal(ok.cpu().numpy().view(np.uint32)[:runs], ek)
+        assert np.array_equal(osum.cpu().numpy().view(np.uint64)[:runs], es)
+        assert np.array_equal(ocnt.cpu().numpy().view(np.uint32)[:runs], ec)
+        assert np.array_equal(dk.cpu().numpy().view(np.uint32), sorted_keys)
