@@ -50,6 +50,7 @@ METRIC = "segsort Gkeys/s vs segment size, % HBM roofline; batched/served p50/p9
 WORKLOAD = ("equal-segment sweep: 2^24 uint32 key/value pairs per instance, keys uniform "
             "in [0,2^32), values = index, segment length 2^1..2^20 (one instance each)")
 BYTES_PER_PAIR = 16  # read key+value once, write key+value once
+STREAM_MAX_AVG = 32  # the library's streamed-tile threshold (segsort_api.cu)
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -511,11 +512,16 @@ def run_ours(args) -> None:
     # key and value once in every call (it sorts the short segments and forms
     # the sorted runs of the long ones) and reads the offsets; each merge pass
     # reads and writes every key and value of the long segments once.
+    # The library runs the streamed tile kernel when the average segment is at
+    # most STREAM_MAX_AVG long, the one-CTA-per-tile kernel otherwise.
     tile_bytes = {lg: BYTES_PER_PAIR * n + 4 * (n // (1 << lg) + 1) for lg in lengths}
+    stream_bytes = {lg: b for lg, b in tile_bytes.items() if (1 << lg) <= STREAM_MAX_AVG}
+    plain_bytes = {lg: b for lg, b in tile_bytes.items() if (1 << lg) > STREAM_MAX_AVG}
     merge_bytes = {lg: BYTES_PER_PAIR * n * merge_passes(1 << lg) for lg in lengths
                    if (1 << lg) > cap}
     kernels = {}
-    for name, table, key in (("tile_sort_kernel", tile_bytes, "tile_ms"),
+    for name, table, key in (("tile_sort_kernel", plain_bytes, "tile_ms"),
+                             ("tile_stream_kernel", stream_bytes, "tile_ms"),
                              ("merge_sort_kernel", merge_bytes, "large_ms")):
         ms_sum = sum(phase[lg][key] for lg in table)
         byts = sum(table.values())

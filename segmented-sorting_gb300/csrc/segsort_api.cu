@@ -38,6 +38,14 @@ cudaEvent_t prof_event(cudaStream_t stream) {
   return e;
 }
 
+// Problems whose average segment is at most this long take the streamed tile
+// kernel (measured on GB300 over 2^24 pairs: faster up to 32, slower from 64).
+// Build-time knob; a huge value sends every multi-tile problem through it.
+#ifndef SEGSORT_STREAM_MAX_AVG
+#define SEGSORT_STREAM_MAX_AVG 32
+#endif
+constexpr int64_t kStreamMaxAvgLen = SEGSORT_STREAM_MAX_AVG;
+
 // ---------------------------------------------------------------------------
 template <typename K, bool PAIRS>
 int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_t nseg,
@@ -108,10 +116,31 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
 
     // ---- tile sort: every segment of at most CAP elements, and the sorted
-    // CAP-runs of the longer ones -------------------------------------------------
+    // CAP-runs of the longer ones.  Short segments on average: the streamed
+    // kernel (persistent CTAs that copy the next tile in while they sort this
+    // one; the load latency dominates there).  Otherwise one CTA per tile: the
+    // sort dominates, and the hardware scheduler balances the tiles better
+    // than a static split over resident CTAs.
     if (prof) rec.t0 = prof_event(stream);
-    tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
-        keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals);
+    if (n <= kStreamMaxAvgLen * static_cast<int64_t>(nseg)) {
+      using SL = StreamLayout<Cfg, K, PAIRS>;
+      auto stream_kernel =
+          tile_stream_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
+      static std::atomic<uint64_t> stream_attr_done{0};
+      static std::atomic<int> stream_occ[kMaxDevices];
+      if (ensure_smem(stream_kernel, SL::kBytes, stream_attr_done, dev) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      const int so = occupancy(stream_kernel, Cfg::NT, SL::kBytes, stream_occ, dev);
+      const unsigned grid =
+          static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(so) * S->sms, tiles));
+      stream_kernel<<<grid, Cfg::NT, SL::kBytes, stream>>>(keys, vals, off, W.half_first,
+                                                           W.tmp_keys, W.tmp_vals, tiles);
+    } else {
+      tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
+          keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals);
+    }
     if (prof) rec.t1 = prof_event(stream);
     if (cudaGetLastError() != cudaSuccess) {
       rc = SEGSORT_ERR_CUDA;

@@ -14,6 +14,7 @@
 #include "segsort.h"
 #include "segsort_common.cuh"
 #include "tile_sort.cuh"
+#include "tile_stream.cuh"
 #include "classify.cuh"
 #include "merge_sort.cuh"
 

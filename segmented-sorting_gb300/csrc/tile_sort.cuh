@@ -103,6 +103,17 @@ template <> struct WordTraits<uint64_t> {
   }
 };
 
+// Chunks whose sort needs more merge levels than this take the radix path,
+// when it is compiled in (SEGSORT_TILE_RADIX=1).  Off by default: measured on
+// GB300 its random-rank scatter makes it shared-memory bound and slower than
+// the merge levels it replaces.
+#ifndef SEGSORT_TILE_RADIX
+#define SEGSORT_TILE_RADIX 0
+#endif
+#ifndef SEGSORT_MERGE_LEVELS_MAX
+#define SEGSORT_MERGE_LEVELS_MAX 2
+#endif
+
 // ---------------------------------------------------------------------------
 // Shared-memory layout and launch shape of one tile-sort instantiation.
 // ---------------------------------------------------------------------------
@@ -133,7 +144,7 @@ struct TileConfig {
   static constexpr size_t kValBytes = PAIRS ? CAP * sizeof(uint32_t) : 0;
   // Radix path (32-bit keys): per-thread digit counters, 16 digits x NT.
   static constexpr bool kRadix = sizeof(Bits) == 4;
-  static constexpr size_t kCntBytes = kRadix ? 16 * NT * sizeof(uint32_t) : 0;
+  static constexpr size_t kCntBytes = (kRadix && SEGSORT_TILE_RADIX) ? 16 * NT * sizeof(uint32_t) : 0;
   static constexpr size_t kSmemBytes = kMainBytes + kValBytes + kCntBytes;
 
   static __device__ __forceinline__ int wslot(int i) { return i + i / WUNIT; }
@@ -303,6 +314,37 @@ __device__ __forceinline__ int block_exclusive_max(int v, int *warp_s) {
   return before;
 }
 
+// In one pass: the exclusive running maximum of a over the threads of the CTA
+// (-1 for thread 0) and the maximum of b (-1 when every b is -1).  warp_s
+// holds 2 * NT / 32 ints.
+template <int NT>
+__device__ __forceinline__ void block_exmax_max(int a, int b, int &a_before, int &b_max,
+                                                int *warp_s) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = a;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x = max(x, y);
+  }
+  int before = __shfl_up_sync(0xFFFFFFFFu, x, 1);
+  if (lane == 0) before = -1;
+  const int bw = static_cast<int>(__reduce_max_sync(0xFFFFFFFFu, static_cast<unsigned>(b + 1))) - 1;
+  if (lane == 31) warp_s[warp] = x;
+  if (lane == 0) warp_s[NW + warp] = bw;
+  __syncthreads();
+  int r = -1;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    if (w < warp) before = max(before, warp_s[w]);
+    r = max(r, warp_s[NW + w]);
+  }
+  __syncthreads();
+  a_before = before;
+  b_max = r;
+}
+
 // Block-wide sum (exclusive prefix and total) of one value per thread.
 template <int NT>
 __device__ __forceinline__ uint32_t block_exclusive_add(uint32_t v, uint32_t &total, int *warp_s) {
@@ -453,16 +495,47 @@ __device__ __forceinline__ void write_chunk(const typename Cfg::Word (&w)[Cfg::K
   __syncthreads();
 }
 
-// Chunks whose sort needs more merge levels than this take the radix path,
-// when it is compiled in (SEGSORT_TILE_RADIX=1).  Off by default: measured on
-// GB300 its random-rank scatter makes it shared-memory bound and slower than
-// the merge levels it replaces.
-#ifndef SEGSORT_TILE_RADIX
-#define SEGSORT_TILE_RADIX 0
-#endif
-#ifndef SEGSORT_MERGE_LEVELS_MAX
-#define SEGSORT_MERGE_LEVELS_MAX 2
-#endif
+
+// ---------------------------------------------------------------------------
+// The element sinks a chunk loader feeds: key i of the chunk becomes word i
+// (order bits, chunk index) in W, value i goes to Vs, and segment heads set
+// bits of the head bitmask hb.
+// ---------------------------------------------------------------------------
+template <typename Cfg, typename K>
+struct ChunkSinks {
+  unsigned char *smem;
+  uint32_t *hb;
+  int m;
+  __device__ __forceinline__ void key(int i, K k) const {
+    reinterpret_cast<typename Cfg::Word *>(smem)[Cfg::wslot(i)] =
+        Cfg::WT::make(Cfg::Ord::to_bits(k), static_cast<uint32_t>(i));
+  }
+  __device__ __forceinline__ void val(int i, uint32_t v) const {
+    reinterpret_cast<uint32_t *>(smem + Cfg::kMainBytes)[i] = v;
+  }
+  __device__ __forceinline__ void head(int64_t p) const {
+    if (p >= 0 && p < m) atomicOr(&hb[p >> 5], 1u << (p & 31));
+  }
+};
+
+// Clears the head bitmask of a chunk of several segments; the caller
+// synchronises before the loader runs.
+template <int NT>
+__device__ __forceinline__ void clear_heads(uint32_t *hb, int m, bool multi) {
+  if (multi)
+    for (int i = threadIdx.x; i < (m + 31) / 32; i += NT) hb[i] = 0;
+}
+
+template <typename Cfg, bool PAIRS, typename K, typename Dst>
+__device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsigned char *smem,
+                                            uint32_t *hb, int *warp_s);
+
+// Destination arrays of a sorted chunk.
+template <typename K>
+struct ChunkDst {
+  K *dst_keys;
+  uint32_t *dst_vals;
+};
 
 // ---------------------------------------------------------------------------
 // Sorts one chunk of m <= CAP elements: reads src_keys/src_vals[0, m), writes
@@ -477,6 +550,32 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
                                            K *dst_keys, uint32_t *dst_vals, int m, bool multi,
                                            Heads &&heads, unsigned char *smem, uint32_t *hb,
                                            int *warp_s) {
+  constexpr int NT = Cfg::NT;
+  clear_heads<NT>(hb, m, multi);
+  if (multi) __syncthreads();
+  // ---- load: keys -> words, values -> Vs, segment heads -> bitmask ----------
+  const ChunkSinks<Cfg, K> S{smem, hb, m};
+  auto fk = [&](int i, K k) { S.key(i, k); };
+  auto fv = [&](int i, uint32_t v) { S.val(i, v); };
+  if constexpr (PAIRS && sizeof(K) == 4) {
+    load_pairs<NT, 4>(src_keys, src_vals, m, fk, fv);
+  } else {
+    load_range<NT, 4>(src_keys, m, fk);
+    if constexpr (PAIRS) load_range<NT, 4>(src_vals, m, fv);
+  }
+  if (multi) heads([&](int64_t p) { S.head(p); });
+  __syncthreads();
+  sort_loaded<Cfg, PAIRS, K>([&] { return ChunkDst<K>{dst_keys, dst_vals}; }, m, multi, smem, hb,
+                             warp_s);
+}
+
+// The sort proper of a loaded chunk: W holds word i at slot wslot(i), Vs the
+// values, hb the segment heads (when multi); every thread has passed a
+// barrier since the loads.  dst() gives the destination (members dst_keys,
+// dst_vals); it is called when the sorted chunk is written.
+template <typename Cfg, bool PAIRS, typename K, typename Dst>
+__device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsigned char *smem,
+                                            uint32_t *hb, int *warp_s) {
   using Ord = typename Cfg::Ord;
   using WT = typename Cfg::WT;
   using Word = typename Cfg::Word;
@@ -487,29 +586,6 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
   uint32_t *VO = reinterpret_cast<uint32_t *>(smem + Cfg::OSLOTS * sizeof(K));
   uint32_t *Vs = reinterpret_cast<uint32_t *>(smem + Cfg::kMainBytes);
   const int tid = threadIdx.x;
-
-  if (multi) {
-    for (int i = tid; i < (m + 31) / 32; i += NT) hb[i] = 0;
-    __syncthreads();
-  }
-  // ---- load: keys -> words, values -> Vs, segment heads -> bitmask ----------
-  auto fk = [&](int i, K k) {
-    W[Cfg::wslot(i)] = WT::make(Ord::to_bits(k), static_cast<uint32_t>(i));
-  };
-  auto fv = [&](int i, uint32_t v) { Vs[i] = v; };
-  if constexpr (PAIRS && sizeof(K) == 4) {
-    load_pairs<NT, 4>(src_keys, src_vals, m, fk, fv);
-  } else {
-    load_range<NT, 4>(src_keys, m, fk);
-    if constexpr (PAIRS) load_range<NT, 4>(src_vals, m, fv);
-  }
-  if (multi) {
-    heads([&](int64_t p) {
-      if (p >= 0 && p < m) atomicOr(&hb[p >> 5], 1u << (p & 31));
-    });
-  }
-  __syncthreads();
-
   const int base = tid * KPT;
 
   // ---- path choice: merge levels this chunk needs ------------------------------
@@ -572,20 +648,31 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
         }
       }
       __syncthreads();
-      store_range<NT>(dst_keys, m, [&](int i) { return KO[Cfg::oslot(i)]; });
-      if constexpr (PAIRS) store_range<NT>(dst_vals, m, [&](int i) { return VO[Cfg::oslot(i)]; });
+      const auto out = dst();
+      store_range<NT>(out.dst_keys, m, [&](int i) { return KO[Cfg::oslot(i)]; });
+      if constexpr (PAIRS)
+        store_range<NT>(out.dst_vals, m, [&](int i) { return VO[Cfg::oslot(i)]; });
       __syncthreads();
       return;
     }
   }
 
   // ---- blocked words + segment field ------------------------------------------
+  // The merge at level l joins runs of KPT * 2^l words and has work only where
+  // one of its run boundaries -- an odd multiple of KPT * 2^l, i.e. the first
+  // position of a thread t with ctz(t) = l -- falls inside a segment.  A chunk
+  // of several segments runs only the levels up to the highest such one (none
+  // at all when every thread's first position starts a segment).
   Word w[KPT];
+  int levels = 31;
   if (multi) {
     constexpr uint32_t kLow = KPT >= 32 ? 0xFFFFFFFFu : ((1u << KPT) - 1);
     const uint32_t mask = base < m ? (hb[base >> 5] >> (base & 31)) & kLow : 0u;
     const int mylast = mask ? base + 31 - __clz(mask) : -1;
-    const int carry = block_exclusive_max<NT>(mylast, warp_s);
+    const int need = (tid > 0 && base < m && !(mask & 1u)) ? __ffs(tid) - 1 : -1;
+    int carry, top;
+    block_exmax_max<NT>(mylast, need, carry, top, warp_s);
+    levels = top + 1;
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
       const int i = base + j;
@@ -608,17 +695,6 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
   thread_sort<WT, KPT>(w);
 
   // ---- merge levels ---------------------------------------------------------------
-  // The level merging runs of KPT * 2^l words has work only where one of its
-  // run boundaries -- an odd multiple of KPT * 2^l, i.e. the first position of
-  // a thread t with ctz(t) = l -- falls inside a segment.  A chunk of several
-  // segments runs only the levels up to the highest such one (none at all
-  // when every thread's first position starts a segment).
-  int levels = 31;
-  if (multi) {
-    int need = -1;
-    if (tid > 0 && base < m && !((hb[base >> 5] >> (base & 31)) & 1u)) need = __ffs(tid) - 1;
-    levels = block_max<NT>(need, warp_s) + 1;
-  }
   bool dirty = true;  // W does not hold this thread's current words
   int level = 0;
   for (int run = KPT; run < m && level < levels; run <<= 1, ++level) {
@@ -707,7 +783,8 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
     }
   }
   __syncthreads();
-  write_chunk<Cfg, PAIRS>(w, m, smem, dst_keys, dst_vals);
+  const auto out = dst();
+  write_chunk<Cfg, PAIRS>(w, m, smem, out.dst_keys, out.dst_vals);
 }
 
 // Merge passes a long segment of len elements needs after its CAP-runs are
@@ -719,18 +796,133 @@ __host__ __device__ __forceinline__ int merge_passes(int64_t len, int64_t cap) {
 }
 
 // ---------------------------------------------------------------------------
-// One CTA of the tile sort: tile t of a problem whose half-tile map is
-// half_first (null: the problem is one tile, n <= CAP, and the CTA sorts one
-// chunk with every segment).
+// The chunks of one tile.  A chunk is m elements from element a on; lo < hi:
+// it holds the segments [lo, hi) (several when hi - lo > 1); lo == hi: it is
+// a CAP-run of long segment lo; tmp: its result goes to the temporary
+// buffers (the buffer the segment's first merge pass reads).
+// ---------------------------------------------------------------------------
+constexpr int kMaxTileChunks = 5;
+struct TileChunk {
+  int64_t a;
+  int32_t lo, hi, m, tmp;
+};
+struct TilePlan {
+  TileChunk c[kMaxTileChunks];
+  int32_t nc;
+};
+
+// The chunk list of tile t of a problem whose half-tile map is half_first
+// (null: the problem is one tile, n <= CAP, and the plan is one chunk with
+// every segment).  runs: the caller forms the CAP-runs of long segments.
 //
-// With tmp_keys given, the CTA also forms the sorted runs of long segments
-// (longer than CAP) for the merge passes: every CAP-chunk [b + k*CAP, ...) of
-// such a segment is sorted by the CTA of the tile its first element lies in,
-// into the buffer the segment's first merge pass reads (the caller's
-// buffers when the segment needs an even number of passes, tmp otherwise, so
-// that its last pass writes the caller's buffers).  A tile holds at most one
-// such chunk of the segment running into it and the first chunk of at most
-// one long segment starting in each of its halves.
+// With runs, the plan also holds the sorted runs of long segments (longer
+// than CAP) for the merge passes: every CAP-chunk [b + k*CAP, ...) of such a
+// segment is sorted by the CTA of the tile its first element lies in, into
+// the buffer the segment's first merge pass reads (the caller's buffers when
+// the segment needs an even number of passes, tmp otherwise, so that its last
+// pass writes the caller's buffers).  A tile holds at most one such chunk of
+// the segment running into it and the first chunk of at most one long
+// segment starting in each of its halves.  One thread computes a plan.
+template <int CAP>
+__device__ __forceinline__ void plan_tile(const Offsets &off, const int32_t *__restrict__ half_first,
+                                          int64_t t, bool runs, TilePlan &P) {
+  constexpr int64_t HALF = CAP / 2;
+  const int64_t nseg = off.nseg;
+  int nc = 0;
+  auto add = [&](int64_t lo, int64_t hi) {
+    if (hi <= lo) return;
+    const int64_t a = off(lo);
+    const int64_t m = off(hi) - a;
+    if (m <= 0 || m > CAP) return;
+    P.c[nc] = TileChunk{a, static_cast<int32_t>(lo), static_cast<int32_t>(hi),
+                        static_cast<int32_t>(m), 0};
+    ++nc;
+  };
+  // The CAP-chunk of long segment s that starts at c.
+  auto add_run = [&](int64_t s, int64_t c) {
+    if (!runs) return;
+    const int64_t b = off(s), e = off(s + 1);
+    if (e - b <= CAP || c < b || c >= e) return;
+    P.c[nc] = TileChunk{c, static_cast<int32_t>(s), static_cast<int32_t>(s),
+                        static_cast<int32_t>(min(static_cast<int64_t>(CAP), e - c)),
+                        merge_passes(e - b, CAP) & 1};
+    ++nc;
+  };
+  if (half_first == nullptr) {
+    add(0, nseg);
+  } else if (t * CAP < off.n) {
+    auto clampi = [&](int64_t v, int64_t lo) { return v < lo ? lo : (v > nseg ? nseg : v); };
+    const int64_t h0 = clampi(__ldg(half_first + 2 * t), 0);
+    const int64_t h1 = clampi(__ldg(half_first + 2 * t + 1), h0);
+    const int64_t h2 = clampi(__ldg(half_first + 2 * t + 2), h1);
+    // A long segment that starts before the tile and runs into it.
+    if (runs && h0 > 0) {
+      const int64_t b = off(h0 - 1), e = off(h0), t0 = t * CAP;
+      if (e - b > CAP && b < t0 && e > t0) {
+        const int64_t c = b + (t0 - b + CAP - 1) / CAP * CAP;
+        if (c < e && c < t0 + CAP) add_run(h0 - 1, c);
+      }
+    }
+    // A last segment of a half-tile longer than HALF is a chunk of its own,
+    // or, when longer than CAP, a long segment whose first run starts here.
+    const bool big_a = h1 > h0 && off(h1) - off(h1 - 1) > HALF;
+    const bool big_b = h2 > h1 && off(h2) - off(h2 - 1) > HALF;
+    const int64_t end_a = big_a ? h1 - 1 : h1;
+    const int64_t end_b = big_b ? h2 - 1 : h2;
+    if (!big_a && off(end_b) - off(h0) <= CAP) {
+      add(h0, end_b);  // both halves' short segments in one chunk
+    } else {
+      add(h0, end_a);
+      if (big_a) {
+        add(h1 - 1, h1);
+        add_run(h1 - 1, off(h1 - 1));
+      }
+      add(h1, end_b);
+    }
+    if (big_b) {
+      add(h2 - 1, h2);
+      add_run(h2 - 1, off(h2 - 1));
+    }
+  }
+  P.nc = nc;
+}
+
+// Where chunk C of a tile reads and writes.
+template <typename K, bool PAIRS>
+struct ChunkIO {
+  const K *src_keys;
+  const uint32_t *src_vals;
+  K *dst_keys;
+  uint32_t *dst_vals;
+  __device__ __forceinline__ ChunkIO(const TileChunk &C, K *keys, uint32_t *vals, K *tmp_keys,
+                                     uint32_t *tmp_vals) {
+    src_keys = keys + C.a;
+    src_vals = PAIRS ? vals + C.a : nullptr;
+    dst_keys = (C.tmp ? tmp_keys : keys) + C.a;
+    dst_vals = PAIRS ? (C.tmp ? tmp_vals : vals) + C.a : nullptr;
+  }
+};
+
+// Sorts chunk C of a tile with loads straight from global memory.
+template <typename Cfg, bool PAIRS, typename K>
+__device__ __forceinline__ void sort_tile_chunk(const TileChunk &C, K *keys, uint32_t *vals,
+                                                const Offsets &off, K *tmp_keys,
+                                                uint32_t *tmp_vals, unsigned char *smem,
+                                                uint32_t *hb, int *warp_s) {
+  const ChunkIO<K, PAIRS> io(C, keys, vals, tmp_keys, tmp_vals);
+  const int64_t a = C.a, lo = C.lo, hi = C.hi;
+  sort_chunk<Cfg, PAIRS>(io.src_keys, io.src_vals, io.dst_keys, io.dst_vals, C.m, hi - lo > 1,
+                         [&](auto &&set) {
+                           for (int64_t j = lo + threadIdx.x; j < hi; j += Cfg::NT)
+                             set(off(j) - a);
+                         },
+                         smem, hb, warp_s);
+}
+
+// ---------------------------------------------------------------------------
+// One CTA of the tile sort: tile t of a problem whose half-tile map is
+// half_first (null: the problem is one tile).  With tmp_keys given the CTA
+// also forms the CAP-runs of long segments (plan_tile).
 // ---------------------------------------------------------------------------
 template <typename K, bool PAIRS, int NT, int KPT>
 __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restrict__ vals,
@@ -738,101 +930,18 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
                                          int64_t t, K *__restrict__ tmp_keys = nullptr,
                                          uint32_t *__restrict__ tmp_vals = nullptr) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
-  constexpr int CAP = Cfg::CAP;
-  constexpr int64_t HALF = Cfg::HALF;
-  constexpr int kMaxChunks = 5;
-
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int64_t chunk_s[kMaxChunks][3];  // a, lo, hi (lo = hi: a long-segment run)
-  __shared__ int32_t chunk_m[kMaxChunks];
-  __shared__ int32_t chunk_tmp[kMaxChunks];   // the run goes to tmp
-  __shared__ int nchunks_s;
-  __shared__ uint32_t hb[CAP / 32];
-  __shared__ int warp_s[NT / 32];
+  __shared__ TilePlan plan_s;
+  __shared__ uint32_t hb[Cfg::CAP / 32];
+  __shared__ int warp_s[NT / 16];
 
-  const int tid = threadIdx.x;
-  const int64_t n = off.n;
-  const int64_t nseg = off.nseg;
-  if (t * CAP >= n) return;
-
-  if (tid == 0) {
-    int nc = 0;
-    auto add = [&](int64_t lo, int64_t hi) {
-      if (hi <= lo) return;
-      const int64_t a = off(lo);
-      const int64_t m = off(hi) - a;
-      if (m <= 0 || m > CAP) return;
-      chunk_s[nc][0] = a;
-      chunk_s[nc][1] = lo;
-      chunk_s[nc][2] = hi;
-      chunk_m[nc] = static_cast<int32_t>(m);
-      chunk_tmp[nc] = 0;
-      ++nc;
-    };
-    // The CAP-chunk of long segment s that starts at c.
-    auto add_run = [&](int64_t s, int64_t c) {
-      if (tmp_keys == nullptr) return;
-      const int64_t b = off(s), e = off(s + 1);
-      if (e - b <= CAP || c < b || c >= e) return;
-      chunk_s[nc][0] = c;
-      chunk_s[nc][1] = s;
-      chunk_s[nc][2] = s;
-      chunk_m[nc] = static_cast<int32_t>(min(static_cast<int64_t>(CAP), e - c));
-      chunk_tmp[nc] = merge_passes(e - b, CAP) & 1;
-      ++nc;
-    };
-    if (half_first == nullptr) {
-      add(0, nseg);
-    } else {
-      auto clampi = [&](int64_t v, int64_t lo) { return v < lo ? lo : (v > nseg ? nseg : v); };
-      const int64_t h0 = clampi(__ldg(half_first + 2 * t), 0);
-      const int64_t h1 = clampi(__ldg(half_first + 2 * t + 1), h0);
-      const int64_t h2 = clampi(__ldg(half_first + 2 * t + 2), h1);
-      // A long segment that starts before the tile and runs into it.
-      if (tmp_keys != nullptr && h0 > 0) {
-        const int64_t b = off(h0 - 1), e = off(h0), t0 = t * CAP;
-        if (e - b > CAP && b < t0 && e > t0) {
-          const int64_t c = b + (t0 - b + CAP - 1) / CAP * CAP;
-          if (c < e && c < t0 + CAP) add_run(h0 - 1, c);
-        }
-      }
-      // A last segment of a half-tile longer than HALF is a chunk of its own,
-      // or, when longer than CAP, a long segment whose first run starts here.
-      const bool big_a = h1 > h0 && off(h1) - off(h1 - 1) > HALF;
-      const bool big_b = h2 > h1 && off(h2) - off(h2 - 1) > HALF;
-      const int64_t end_a = big_a ? h1 - 1 : h1;
-      const int64_t end_b = big_b ? h2 - 1 : h2;
-      if (!big_a && off(end_b) - off(h0) <= CAP) {
-        add(h0, end_b);  // both halves' short segments in one chunk
-      } else {
-        add(h0, end_a);
-        if (big_a) {
-          add(h1 - 1, h1);
-          add_run(h1 - 1, off(h1 - 1));
-        }
-        add(h1, end_b);
-      }
-      if (big_b) {
-        add(h2 - 1, h2);
-        add_run(h2 - 1, off(h2 - 1));
-      }
-    }
-    nchunks_s = nc;
-  }
+  if (t * Cfg::CAP >= off.n) return;
+  if (threadIdx.x == 0) plan_tile<Cfg::CAP>(off, half_first, t, tmp_keys != nullptr, plan_s);
   __syncthreads();
-  const int nc = nchunks_s;
-  for (int c = 0; c < nc; ++c) {
-    const int64_t a = chunk_s[c][0], lo = chunk_s[c][1], hi = chunk_s[c][2];
-    K *k = keys + a;
-    uint32_t *v = PAIRS ? vals + a : nullptr;
-    K *dk = chunk_tmp[c] ? tmp_keys + a : k;
-    uint32_t *dv = PAIRS ? (chunk_tmp[c] ? tmp_vals + a : v) : nullptr;
-    sort_chunk<Cfg, PAIRS>(k, v, dk, dv, chunk_m[c], hi - lo > 1,
-                           [&](auto &&set) {
-                             for (int64_t j = lo + tid; j < hi; j += NT) set(off(j) - a);
-                           },
-                           smem, hb, warp_s);
-  }
+  const int nc = plan_s.nc;
+  for (int c = 0; c < nc; ++c)
+    sort_tile_chunk<Cfg, PAIRS>(plan_s.c[c], keys, vals, off, tmp_keys, tmp_vals, smem, hb,
+                                warp_s);
 }
 
 // ---------------------------------------------------------------------------

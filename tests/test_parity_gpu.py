@@ -221,6 +221,52 @@ def test_edge_cases(pkg, cuda, oracle, inst):
     check_both(pkg, cuda, oracle, keys[:9000], np.array([-50, 3000, 8000, 123456], np.int32))
 
 
+def test_keys_and_values_aligned_differently(pkg, cuda, oracle, inst):
+    """Keys and values at different offsets from a 16-byte boundary, over many
+    tiles: each array's staged middle and ragged ends are found separately."""
+    torch = cuda
+    L = pkg.lib()
+    n = 50000
+    st = torch.cuda.current_stream().cuda_stream
+    for kshift, vshift in ((1, 2), (3, 0), (0, 1), (2, 3)):
+        for off in (inst.lognormal_offsets(n, seed=20 + kshift, empty_frac=0.05),
+                    inst.equal_offsets_ragged(n, 7 + kshift * 300)):
+            keys = inst.uniform_keys(n, seed=30 + kshift, bits=12)
+            vals = np.arange(n, dtype=np.uint32)
+            kb = torch.full((n + 8,), -1, dtype=torch.int32, device="cuda")
+            vb = torch.full((n + 8,), -2, dtype=torch.int32, device="cuda")
+            kb[kshift:kshift + n] = torch.from_numpy(keys.view(np.int32)).cuda()
+            vb[vshift:vshift + n] = torch.from_numpy(vals.view(np.int32)).cuda()
+            dof = torch.from_numpy(off).cuda()
+            rc = L.segsort_pairs_u32(kb.data_ptr() + 4 * kshift, vb.data_ptr() + 4 * vshift, n,
+                                     dof.data_ptr(), len(off) - 1, st)
+            assert rc == pkg.SEGSORT_OK
+            torch.cuda.synchronize()
+            assert pkg.device_status() == pkg.SEGSORT_OK
+            k = kb.cpu().numpy().view(np.uint32)
+            v = vb.cpu().numpy().view(np.uint32)
+            ek, ev = oracle.segsort_numpy(keys, off, vals)
+            assert np.array_equal(k[kshift:kshift + n], ek), first_diff(k[kshift:kshift + n], ek)
+            assert np.array_equal(v[vshift:vshift + n], ev), first_diff(v[vshift:vshift + n], ev)
+            assert np.all(k[:kshift] == 0xFFFFFFFF) and np.all(k[kshift + n:] == 0xFFFFFFFF)
+            assert np.all(v[:vshift] == 0xFFFFFFFE) and np.all(v[vshift + n:] == 0xFFFFFFFE)
+
+
+def test_dense_segment_starts_across_tiles(pkg, cuda, oracle, inst):
+    """Tiles whose chunks hold more segment starts than elements: runs of
+    length-1 segments and thousands of empty segments inside a multi-tile
+    problem, between short and long ones."""
+    rng = np.random.default_rng(21)
+    lens = np.concatenate([np.ones(10000), np.zeros(5000), rng.integers(0, 9, 8000),
+                           np.zeros(3000), [9000], np.full(2000, 3), np.zeros(4500), [2],
+                           np.ones(6000)]).astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    n = int(off[-1])
+    for bits in (32, 2):
+        check_both(pkg, cuda, oracle, inst.uniform_keys(n, seed=22 + bits, bits=bits), off)
+    check_both(pkg, cuda, oracle, inst.uniform_keys(n, seed=23, bits=5), off[:-1], heads=True)
+
+
 def test_repeated_calls_are_idempotent(pkg, cuda, oracle, inst):
     n = 1 << 17
     off = inst.lognormal_offsets(n, seed=17)
