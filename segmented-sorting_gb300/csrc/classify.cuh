@@ -92,6 +92,113 @@ large_classify_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
   classify_boundary<K>(off, s, true, cap, half, ws.half_first, ws.halves, ws, 0);
 }
 
+// The first segment s in [0, nseg] with off(s) >= x, counting off(nseg) as
+// +inf (offsets are non-decreasing).  Called by a whole warp; every round
+// probes 32 points of the remaining interval, so a search over 2^23 segments
+// takes 5 rounds of loads.
+__device__ __forceinline__ int64_t warp_lower_bound(const Offsets &off, int64_t x) {
+  const int lane = threadIdx.x & 31;
+  int64_t lo = 0, hi = off.nseg;  // the answer lies in [lo, hi]
+  while (hi > lo) {
+    const int64_t span = hi - lo;
+    const bool small = span <= 32;
+    // Probes lie in [lo, hi), so they read offsets below nseg only.
+    const int64_t p = small ? lo + lane : lo + (span * (lane + 1)) / 33;
+    const bool ge = (small && lane >= span) ? true : off(p) >= x;
+    const int c = __popc(~__ballot_sync(0xFFFFFFFFu, ge));  // lanes below the first true one
+    if (small) {
+      lo += c;
+      hi = lo;
+    } else {
+      const long long before = __shfl_sync(0xFFFFFFFFu, static_cast<long long>(p), c > 0 ? c - 1 : 0);
+      const long long at = __shfl_sync(0xFFFFFFFFu, static_cast<long long>(p), c < 32 ? c : 31);
+      const int64_t nlo = c > 0 ? before + 1 : lo;
+      const int64_t nhi = c < 32 ? at : hi;
+      lo = nlo;
+      hi = nhi;
+    }
+  }
+  return lo;
+}
+
+// Classify by half-tiles (one problem): half_first[h] -- the lower bound of
+// h * half in the offsets, the same map classify_boundary writes -- for h in
+// [0, halves], and the one segment that can be long among those starting in
+// half-tile h: the last one, half_first[h + 1] - 1.  A segment longer than
+// cap >= half runs past the end of the half-tile it starts in, so no other
+// segment starts after it there, and every long segment is found once, by
+// the half-tile it starts in.  Work grows with the number of half-tiles, not
+// segments.  A CTA of kClassifyWarps + 1 warps handles kClassifyWarps
+// entries, one search per warp: the extra warp finds the next CTA's first
+// entry, which the CTA's last job check needs.
+constexpr int kClassifyWarps = 8;
+
+template <typename K>
+__global__ void __launch_bounds__((kClassifyWarps + 1) * 32)
+large_classify_halves_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
+  __shared__ int64_t lb_s[kClassifyWarps + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t h = static_cast<int64_t>(blockIdx.x) * kClassifyWarps + w;
+  if (h <= ws.halves) {
+    const int64_t a = warp_lower_bound(off, h * half);
+    if (lane == 0) {
+      lb_s[w] = a;
+      if (w < kClassifyWarps) ws.half_first[h] = static_cast<int32_t>(a);
+    }
+  }
+  __syncthreads();
+  if (w < kClassifyWarps && h < ws.halves && lane == 0) {
+    const int64_t a = lb_s[w], b = lb_s[w + 1];
+    if (b > a) {
+      const int64_t beg = off(b - 1), end = off(b);
+      if (end - beg > cap) {
+        const uint32_t j = atomicAdd(&ws.ctr[kCtrJobs], 1u);
+        if (j < static_cast<uint32_t>(ws.max_jobs))
+          ws.jobs[j] = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end), 0, 0);
+      }
+    }
+  }
+}
+
+// Batched form of the half-tile classify: global entry g is entry
+// g - half_base of the instance that owns it (each instance owns
+// 2 * tiles + 1 entries).  Entry h + 1 of the job check belongs to the same
+// instance as entry h, since h < 2 * tiles.
+template <typename K>
+__global__ void __launch_bounds__((kClassifyWarps + 1) * 32)
+large_classify_halves_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
+                                   int64_t entries, int64_t cap, int64_t half, LargeWs<K> ws) {
+  __shared__ int64_t lb_s[kClassifyWarps + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t g = static_cast<int64_t>(blockIdx.x) * kClassifyWarps + w;
+  int32_t i = 0;
+  int64_t h = 0, halves = 0;
+  if (g < entries) {
+    i = find_instance(tab, count, g, &BatchInst::half_base);
+    const BatchInst &I = tab[i];
+    h = g - I.half_base;
+    halves = 2 * ((I.n + cap - 1) / cap);
+    const int64_t a = warp_lower_bound(I.offsets_view(), h * half);
+    if (lane == 0) {
+      lb_s[w] = a;
+      if (w < kClassifyWarps) ws.half_first[g] = static_cast<int32_t>(a);
+    }
+  }
+  __syncthreads();
+  if (w < kClassifyWarps && g < entries && h < halves && lane == 0) {
+    const int64_t a = lb_s[w], b = lb_s[w + 1];
+    if (b > a) {
+      const Offsets off = tab[i].offsets_view();
+      const int64_t beg = off(b - 1), end = off(b);
+      if (end - beg > cap) {
+        const uint32_t j = atomicAdd(&ws.ctr[kCtrJobs], 1u);
+        if (j < static_cast<uint32_t>(ws.max_jobs))
+          ws.jobs[j] = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end), 0, i);
+      }
+    }
+  }
+}
+
 // Batched form: thread g classifies boundary g - bound_base of the instance
 // that owns it; `bounds` is the batch's total of nseg + 1 over its instances.
 template <typename K>

@@ -38,9 +38,10 @@ cudaEvent_t prof_event(cudaStream_t stream) {
   return e;
 }
 
-// Problems whose average segment is at most this long take the streamed tile
-// kernel (measured on GB300 over 2^24 pairs: faster up to 32, slower from 64).
-// Build-time knob; a huge value sends every multi-tile problem through it.
+// Problems whose average segment is at most this long take the half-tile
+// classify and the streamed tile kernel (measured on GB300 over 2^24 pairs:
+// both faster up to 32, slower from 64).  Build-time knob; a huge value sends
+// every multi-tile problem through them.
 #ifndef SEGSORT_STREAM_MAX_AVG
 #define SEGSORT_STREAM_MAX_AVG 32
 #endif
@@ -112,8 +113,19 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       rc = SEGSORT_ERR_CUDA;
       break;
     }
-    const unsigned cls_blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 1 + 255) / 256);
-    large_classify_kernel<K><<<cls_blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
+    // Short segments on average: one search per half-tile (work ~ n / CAP);
+    // otherwise one thread per segment boundary (work ~ nseg, fewer rounds
+    // of dependent loads).  The two write the same map and jobs.
+    const bool short_avg = n <= kStreamMaxAvgLen * static_cast<int64_t>(nseg);
+    if (short_avg) {
+      const unsigned blocks =
+          static_cast<unsigned>((W.halves + kClassifyWarps) / kClassifyWarps);  // halves + 1 entries
+      large_classify_halves_kernel<K><<<blocks, (kClassifyWarps + 1) * 32, 0, stream>>>(
+          off, tile_cap<K>(), tile_cap<K>() / 2, W);
+    } else {
+      const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 1 + 255) / 256);
+      large_classify_kernel<K><<<blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
+    }
 
     // ---- tile sort: every segment of at most CAP elements, and the sorted
     // CAP-runs of the longer ones.  Short segments on average: the streamed
@@ -122,7 +134,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // sort dominates, and the hardware scheduler balances the tiles better
     // than a static split over resident CTAs.
     if (prof) rec.t0 = prof_event(stream);
-    if (n <= kStreamMaxAvgLen * static_cast<int64_t>(nseg)) {
+    if (short_avg) {
       using SL = StreamLayout<Cfg, K, PAIRS>;
       auto stream_kernel =
           tile_stream_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;

@@ -147,7 +147,7 @@ struct BatchKernels {
   static constexpr auto tile = tile_sort_batch_kernel<K, true, TCfg::NT, TCfg::KPT,
                                                       TileFor<K, true>::kMinBlocks>;
   static constexpr auto merge = merge_sort_kernel<K, true, BatchSpace<K>>;
-  static constexpr auto classify = large_classify_batch_kernel<K>;
+  static constexpr auto classify = large_classify_halves_batch_kernel<K>;
   static inline std::atomic<uint64_t> tile_attr{0}, merge_attr{0};
   static inline std::atomic<int> merge_occ[kMaxDevices];
 
@@ -167,8 +167,10 @@ struct BatchKernels {
     const int64_t cap = tile_cap<K>();
     if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess)
       return SEGSORT_ERR_CUDA;
-    const unsigned cls_blocks = static_cast<unsigned>((G.bounds + 255) / 256);
-    classify<<<cls_blocks, 256, 0, stream>>>(tab, count, G.bounds, cap, cap / 2, W);
+    const unsigned cls_blocks =
+        static_cast<unsigned>((G.half_entries + kClassifyWarps - 1) / kClassifyWarps);
+    classify<<<cls_blocks, (kClassifyWarps + 1) * 32, 0, stream>>>(tab, count, G.half_entries, cap,
+                                                                   cap / 2, W);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
 
     // Tile sort first: it forms the sorted runs the merge passes read.
