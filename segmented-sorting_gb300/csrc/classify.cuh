@@ -2,12 +2,14 @@
 // shares with the host: the workspace views, the counters, the bounded grid
 // barrier and the mapping of a job's instance to its buffers.
 //
-// Classify (one thread per segment boundary) replaces the reference's length
-// binning bb_bin (src/bb_segsort/bb_bin.h:23,31-139): instead of 13
-// power-of-two bins and a device-to-host copy of their counts (bb_bin.h:46),
-// it writes a half-tile -> first-segment map that the tile sort reads
-// directly, and a device-side list of the segments longer than the tile
-// capacity for the merge passes.
+// Classify replaces the reference's length binning bb_bin
+// (src/bb_segsort/bb_bin.h:23,31-139): instead of 13 power-of-two bins and a
+// device-to-host copy of their counts (bb_bin.h:46), it writes a half-tile ->
+// first-segment map that the tile sort reads directly, and a device-side list
+// of the segments longer than the tile capacity for the merge passes.  Two
+// forms write the same map and list: one thread per segment boundary
+// (problems of long segments on average), or one warp-cooperative search per
+// half-tile (short segments, and batches).
 #pragma once
 
 #include "segsort_common.cuh"
@@ -197,21 +199,6 @@ large_classify_halves_batch_kernel(const BatchInst *__restrict__ tab, int32_t co
       }
     }
   }
-}
-
-// Batched form: thread g classifies boundary g - bound_base of the instance
-// that owns it; `bounds` is the batch's total of nseg + 1 over its instances.
-template <typename K>
-__global__ void __launch_bounds__(256)
-large_classify_batch_kernel(const BatchInst *__restrict__ tab, int32_t count, int64_t bounds,
-                            int64_t cap, int64_t half, LargeWs<K> ws) {
-  const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool valid = g < bounds;
-  const int32_t i = find_instance(tab, count, valid ? g : 0, &BatchInst::bound_base);
-  const BatchInst &I = tab[i];
-  const int64_t tiles = (I.n + cap - 1) / cap;
-  classify_boundary<K>(I.offsets_view(), g - I.bound_base, valid, cap, half,
-                       ws.half_first + I.half_base, 2 * tiles, ws, i);
 }
 
 // ---------------------------------------------------------------------------

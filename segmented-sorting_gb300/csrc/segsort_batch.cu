@@ -4,7 +4,7 @@
 // same three kernels as one plain call -- classify, the tile sort, the
 // cooperative merge passes for long segments -- launched once for the whole
 // group: every kernel finds an instance through a device table (BatchInst),
-// tile-sort CTAs and classify threads by binary search over the instances'
+// tile-sort CTAs and classify warps by binary search over the instances'
 // bases, and long-segment jobs through the instance index they carry.  Small instances
 // therefore share CTAs' worth of work with large ones instead of paying a
 // sequence of launches and grid barriers each.
@@ -39,7 +39,7 @@ constexpr int64_t kGroupMaxN = (int64_t{1} << 31) - 1;
 struct Group {
   int key_type = 0;
   std::vector<BatchInst> insts;  // non-empty instances only
-  int64_t total_n = 0, tiles = 0, bounds = 0, half_entries = 0;
+  int64_t total_n = 0, tiles = 0, half_entries = 0;
   WsLayout L;
   size_t tab_off = 0;  // table position in the batch buffer
   size_t ws_off = 0;   // workspace position in the batch buffer
@@ -87,12 +87,10 @@ int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B)
     I.tmp_base = G.total_n;
     I.half_base = G.half_entries;
     I.tile_base = G.tiles;
-    I.bound_base = G.bounds;
     G.insts.push_back(I);
     G.total_n += it.n;
     G.half_entries += 2 * tiles + 1;
     G.tiles += tiles;
-    G.bounds += static_cast<int64_t>(it.nseg) + 1;
     if (G.total_n > kGroupMaxN) return SEGSORT_ERR_TOO_LARGE;
   }
   size_t off = 0;

@@ -77,8 +77,8 @@ struct Offsets {
 // independent (keys, values, offsets) problems of one key type sorted by one
 // launch of each kernel.  Every per-instance index is instance-local; the
 // *_base fields place the instance in the batch-wide arrays: its region of
-// the temporary key/value buffers, its half-tile map, its tile-sort CTAs and
-// its classify threads (one per segment boundary, nseg + 1 of them).
+// the temporary key/value buffers, its half-tile map (2 * tiles + 1 entries,
+// one classify warp each) and its tile-sort CTAs.
 // ---------------------------------------------------------------------------
 struct BatchInst {
   void *keys;
@@ -88,7 +88,6 @@ struct BatchInst {
   int64_t tmp_base;
   int64_t half_base;
   int64_t tile_base;
-  int64_t bound_base;
   int32_t nseg;
   int32_t heads;
 

@@ -173,6 +173,34 @@ __device__ __forceinline__ void thread_sort(typename WT::T (&w)[KPT]) {
   }
 }
 
+// `rounds` rounds of odd-even transposition over KPT words (even pairs first).
+// Any run of at most `rounds` words is sorted afterwards, whichever parity
+// its first position has, when no exchange crosses its ends.
+template <typename WT, int KPT>
+__device__ __forceinline__ void transposition_sort(typename WT::T (&w)[KPT], int rounds) {
+  auto cas = [](typename WT::T &a, typename WT::T &b) {
+    const typename WT::T x = a, y = b;
+    const bool swap = WT::lt(y, x);
+    a = swap ? y : x;
+    b = swap ? x : y;
+  };
+  for (int r = 0; r < rounds; ++r) {
+    if ((r & 1) == 0) {
+#pragma unroll
+      for (int i = 0; i + 1 < KPT; i += 2) cas(w[i], w[i + 1]);
+    } else {
+#pragma unroll
+      for (int i = 1; i + 1 < KPT; i += 2) cas(w[i], w[i + 1]);
+    }
+  }
+}
+
+// Longest segment (in words) for which the transposition rounds cost fewer
+// exchanges than the bitonic network: about KPT/2 - 1/2 exchanges a round
+// against KPT/2 * log2(KPT) * (log2(KPT) + 1) / 2 for the network.
+template <int KPT>
+constexpr int kTranspositionMaxRounds = KPT >= 16 ? 10 : (KPT >= 8 ? 6 : 2);
+
 // ---------------------------------------------------------------------------
 // Range copies between global memory and per-element callbacks: 16-byte
 // vector accesses for the aligned middle, UNROLL vectors per thread in flight,
@@ -526,7 +554,7 @@ __device__ __forceinline__ void clear_heads(uint32_t *hb, int m, bool multi) {
     for (int i = threadIdx.x; i < (m + 31) / 32; i += NT) hb[i] = 0;
 }
 
-template <typename Cfg, bool PAIRS, typename K, typename Dst>
+template <typename Cfg, bool PAIRS, typename K, bool kShort = false, typename Dst>
 __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsigned char *smem,
                                             uint32_t *hb, int *warp_s);
 
@@ -545,7 +573,7 @@ struct ChunkDst {
 // must call set(p) for the local start p of each segment (any thread, any
 // order, repeats allowed).
 // ---------------------------------------------------------------------------
-template <typename Cfg, bool PAIRS, typename K, typename Heads>
+template <typename Cfg, bool PAIRS, typename K, bool kShort = false, typename Heads>
 __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *src_vals,
                                            K *dst_keys, uint32_t *dst_vals, int m, bool multi,
                                            Heads &&heads, unsigned char *smem, uint32_t *hb,
@@ -565,15 +593,18 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
   }
   if (multi) heads([&](int64_t p) { S.head(p); });
   __syncthreads();
-  sort_loaded<Cfg, PAIRS, K>([&] { return ChunkDst<K>{dst_keys, dst_vals}; }, m, multi, smem, hb,
-                             warp_s);
+  sort_loaded<Cfg, PAIRS, K, kShort>([&] { return ChunkDst<K>{dst_keys, dst_vals}; }, m, multi,
+                                     smem, hb, warp_s);
 }
 
 // The sort proper of a loaded chunk: W holds word i at slot wslot(i), Vs the
 // values, hb the segment heads (when multi); every thread has passed a
 // barrier since the loads.  dst() gives the destination (members dst_keys,
-// dst_vals); it is called when the sorted chunk is written.
-template <typename Cfg, bool PAIRS, typename K, typename Dst>
+// dst_vals); it is called when the sorted chunk is written.  kShort compiles
+// in the transposition rounds for chunks of short segments (the streamed
+// kernel, which runs problems of short segments; kept out of the plain
+// kernel, whose register allocation for the merge levels it disturbs).
+template <typename Cfg, bool PAIRS, typename K, bool kShort, typename Dst>
 __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsigned char *smem,
                                             uint32_t *hb, int *warp_s) {
   using Ord = typename Cfg::Ord;
@@ -665,9 +696,10 @@ __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsign
   // at all when every thread's first position starts a segment).
   Word w[KPT];
   int levels = 31;
+  uint32_t mask = 0;  // segment heads among this thread's positions (bit j: base + j)
   if (multi) {
     constexpr uint32_t kLow = KPT >= 32 ? 0xFFFFFFFFu : ((1u << KPT) - 1);
-    const uint32_t mask = base < m ? (hb[base >> 5] >> (base & 31)) & kLow : 0u;
+    mask = base < m ? (hb[base >> 5] >> (base & 31)) & kLow : 0u;
     const int mylast = mask ? base + 31 - __clz(mask) : -1;
     const int need = (tid > 0 && base < m && !(mask & 1u)) ? __ffs(tid) - 1 : -1;
     int carry, top;
@@ -692,7 +724,33 @@ __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsign
     }
   }
 
-  thread_sort<WT, KPT>(w);
+  // ---- in-register sort ----------------------------------------------------------
+  // Without merge levels no segment crosses a thread's block, and R rounds of
+  // odd-even transposition sort every segment of at most R words (words of
+  // different segments are already in order, so no exchange crosses a
+  // segment's boundary): cheaper than the bitonic network for short ones.
+  int rounds = KPT;
+  if (kShort && levels == 0) {
+    const int lim = base < m ? min(KPT, m - base) : 0;
+    uint32_t rest = (mask | (1u << lim)) & ~1u;  // segment ends after position 0
+    int longest = 0, prev = 0;
+    while (rest) {
+      const int b = __ffs(rest) - 1;
+      longest = max(longest, b - prev);
+      prev = b;
+      rest &= rest - 1;
+    }
+    rounds = static_cast<int>(__reduce_max_sync(0xFFFFFFFFu, static_cast<unsigned>(longest)));
+  }
+  if constexpr (kShort) {
+    if (rounds <= kTranspositionMaxRounds<KPT>) {
+      transposition_sort<WT, KPT>(w, rounds);
+    } else {
+      thread_sort<WT, KPT>(w);
+    }
+  } else {
+    thread_sort<WT, KPT>(w);
+  }
 
   // ---- merge levels ---------------------------------------------------------------
   bool dirty = true;  // W does not hold this thread's current words
@@ -904,14 +962,15 @@ struct ChunkIO {
 };
 
 // Sorts chunk C of a tile with loads straight from global memory.
-template <typename Cfg, bool PAIRS, typename K>
+template <typename Cfg, bool PAIRS, bool kShort = false, typename K>
 __device__ __forceinline__ void sort_tile_chunk(const TileChunk &C, K *keys, uint32_t *vals,
                                                 const Offsets &off, K *tmp_keys,
                                                 uint32_t *tmp_vals, unsigned char *smem,
                                                 uint32_t *hb, int *warp_s) {
   const ChunkIO<K, PAIRS> io(C, keys, vals, tmp_keys, tmp_vals);
   const int64_t a = C.a, lo = C.lo, hi = C.hi;
-  sort_chunk<Cfg, PAIRS>(io.src_keys, io.src_vals, io.dst_keys, io.dst_vals, C.m, hi - lo > 1,
+  sort_chunk<Cfg, PAIRS, K, kShort>(io.src_keys, io.src_vals, io.dst_keys, io.dst_vals, C.m,
+                                    hi - lo > 1,
                          [&](auto &&set) {
                            for (int64_t j = lo + threadIdx.x; j < hi; j += Cfg::NT)
                              set(off(j) - a);

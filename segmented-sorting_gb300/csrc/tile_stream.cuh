@@ -269,10 +269,10 @@ tile_stream_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
     }
     if (nc > 0) {
       const ChunkIO<K, PAIRS> io(C0, keys, vals, tmp_keys, tmp_vals);
-      sort_loaded<Cfg, PAIRS, K>([=] { return io; }, m, multi, smem, hb, warp_s);
+      sort_loaded<Cfg, PAIRS, K, true>([=] { return io; }, m, multi, smem, hb, warp_s);
       for (int c = 1; c < nc; ++c)
-        sort_tile_chunk<Cfg, PAIRS>(P.c[c], keys, vals, off, tmp_keys, tmp_vals, smem, hb,
-                                    warp_s);
+        sort_tile_chunk<Cfg, PAIRS, true>(P.c[c], keys, vals, off, tmp_keys, tmp_vals, smem, hb,
+                                          warp_s);
     }
   }
 }

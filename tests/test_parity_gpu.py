@@ -267,6 +267,28 @@ def test_dense_segment_starts_across_tiles(pkg, cuda, oracle, inst):
     check_both(pkg, cuda, oracle, inst.uniform_keys(n, seed=23, bits=5), off[:-1], heads=True)
 
 
+@pytest.mark.parametrize("dtype,block", [(np.uint32, 16), (np.uint64, 8)])
+def test_segments_within_thread_blocks(pkg, cuda, oracle, inst, dtype, block):
+    """Every block of `block` positions (one thread's words in the tile sort)
+    split into segments of 1..12 elements: no segment crosses a block, so
+    the tile sort uses no merge level and sorts each block's segments in
+    registers (transposition rounds up to the longest segment, or the
+    bitonic network)."""
+    rng = np.random.default_rng(block)
+    lens = []
+    for _ in range(40000 // block):
+        left = block
+        while left:
+            ln = int(min(left, rng.integers(1, 13)))
+            lens.append(ln)
+            left -= ln
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    n = int(off[-1])
+    for bits in (3, 32):
+        keys = inst.uniform_keys(n, seed=40 + bits, bits=bits, dtype=dtype)
+        check_both(pkg, cuda, oracle, keys, off)
+
+
 def test_repeated_calls_are_idempotent(pkg, cuda, oracle, inst):
     n = 1 << 17
     off = inst.lognormal_offsets(n, seed=17)
