@@ -12,9 +12,9 @@
 //
 // One cooperative kernel runs all passes.  A pass has two phases separated
 // by a bounded grid barrier:
-//   partition  one warp per output item (T consecutive outputs of one merge)
-//              finds where the item starts in the two runs (merge path,
-//              32 probes per round over global memory);
+//   partition  one half-warp per output item (T consecutive outputs of one
+//              merge) finds where the item starts in the two runs (merge
+//              path, 16 probes per round over global memory);
 //   merge      one CTA per item loads the two windows the item consumes into
 //              shared memory, each thread merges KPT outputs from its own
 //              merge-path split of the windows, and the CTA stores the item
@@ -72,31 +72,38 @@ struct MergeSmem {
 
 // Merge-path split of diagonal d of the sorted runs A[0, la) and B[0, lb):
 // how many elements of A are among the first d outputs of their merge, ties
-// taken from A first.  Called by a whole warp; every round probes 32 points
-// of the remaining interval.
-template <typename K>
-__device__ __forceinline__ int64_t warp_merge_split(const K *A, int64_t la, const K *B, int64_t lb,
-                                                    int64_t d) {
+// taken from A first.  Called by a group of W lanes (a whole warp, or the
+// aligned half of one); every round probes W points of the remaining
+// interval.
+template <int W, typename K>
+__device__ __forceinline__ int64_t group_merge_split(const K *A, int64_t la, const K *B,
+                                                     int64_t lb, int64_t d) {
+  static_assert(W == 16 || W == 32, "a group is a warp or half of one");
   using Ord = KeyOrder<K>;
   const int lane = threadIdx.x & 31;
+  const int gl = lane & (W - 1);   // lane within the group
+  const int g0 = lane & ~(W - 1);  // the group's first lane
+  const unsigned mask = W == 32 ? 0xFFFFFFFFu : (0xFFFFu << g0);
   int64_t lo = d > lb ? d - lb : 0;
   int64_t hi = d < la ? d : la;
   // The split s is in [lo, hi]; A[i] <= B[d - 1 - i] holds exactly for i < s.
   while (hi > lo) {
     const int64_t span = hi - lo;
-    const bool small = span <= 32;
-    const int64_t mid = small ? lo + lane : lo + (span * (lane + 1)) / 33;
+    const bool small = span <= W;
+    const int64_t mid = small ? lo + gl : lo + (span * (gl + 1)) / (W + 1);
     bool pred = false;
-    if (!small || lane < span) pred = Ord::to_bits(A[mid]) <= Ord::to_bits(B[d - 1 - mid]);
-    const int c = __popc(__ballot_sync(0xFFFFFFFFu, pred));
+    if (!small || gl < span) pred = Ord::to_bits(A[mid]) <= Ord::to_bits(B[d - 1 - mid]);
+    const int c = __popc(__ballot_sync(mask, pred) & mask);
     if (small) {
       lo += c;
       hi = lo;
     } else {
-      const long long last_true = __shfl_sync(0xFFFFFFFFu, static_cast<long long>(mid), c > 0 ? c - 1 : 0);
-      const long long first_false = __shfl_sync(0xFFFFFFFFu, static_cast<long long>(mid), c < 32 ? c : 31);
+      const long long last_true =
+          __shfl_sync(mask, static_cast<long long>(mid), g0 + (c > 0 ? c - 1 : 0));
+      const long long first_false =
+          __shfl_sync(mask, static_cast<long long>(mid), g0 + (c < W ? c : W - 1));
       const int64_t nlo = c > 0 ? last_true + 1 : lo;
-      const int64_t nhi = c < 32 ? first_false : hi;
+      const int64_t nhi = c < W ? first_false : hi;
       lo = nlo;
       hi = nhi;
     }
@@ -163,8 +170,15 @@ __device__ __forceinline__ void load_ranges(const T *const (&src)[R], const int 
 }
 
 // ---------------------------------------------------------------------------
+// Resident CTAs per SM the registers must allow: 3 for 32-bit keys; 2 for
+// 64-bit keys, whose merge at 80 registers spilled 400 bytes a thread
+// (measured on GB300, 2^23 u64 pairs in segments of 2^16: 0.857 ms at 3 CTAs
+// per SM with the spills, 0.797 ms at 2 without).
+template <typename K>
+constexpr int kMergeMinBlocks = sizeof(K) == 8 ? 2 : SEGSORT_MERGE_MINB;
+
 template <typename K, bool PAIRS, typename Space>
-__global__ void __launch_bounds__(kMThreads, SEGSORT_MERGE_MINB)
+__global__ void __launch_bounds__(kMThreads, kMergeMinBlocks<K>)
 merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
   using Ord = KeyOrder<K>;
   using MS = MergeSmem<K, PAIRS>;
@@ -177,7 +191,7 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
   __shared__ uint64_t carry_s;
   __shared__ int maxp_s;
 
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int64_t G = gridDim.x;
   const int64_t nj = min(static_cast<int64_t>(ld_volatile(&ws.ctr[kCtrJobs])),
                          static_cast<int64_t>(ws.max_jobs));
@@ -248,15 +262,19 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
 
   for (int p = 0; p < maxp; ++p) {
     const int64_t R = cap << p;  // run length this pass merges
-    // ---- partition: one warp per item ------------------------------------
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * kMWarps + warp; i < total;
-         i += G * kMWarps) {
+    // ---- partition: one half-warp per item (a grid of 3 CTAs per SM has
+    // more half-warps than a 2^24-pair problem has items, so no group
+    // searches twice) ---------------------------------------------------------
+    constexpr int kGroups = 2 * kMWarps;  // half-warps per CTA
+    const int grp = tid >> 4, gl = tid & 15;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * kGroups + grp; i < total;
+         i += G * kGroups) {
       const int32_t j = item_job[i];
       const int4 jb = jobs[j];
       const int64_t len = jb.y - jb.x;
       const int np = merge_passes(len, cap);
       if (p >= np) {
-        if (lane == 0) desc[2 * i + 1] = make_int4(jb.w, 0, 0, 0);
+        if (gl == 0) desc[2 * i + 1] = make_int4(jb.w, 0, 0, 0);
         continue;
       }
       const int64_t o = (i - item_prefix[j]) * static_cast<int64_t>(T);
@@ -266,8 +284,9 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
       const SideBuffers<K> B = sp(jb.w);
       const int from_tmp = (np - p) & 1;
       const K *src = from_tmp ? B.tmp_keys : B.keys;
-      const int64_t s = warp_merge_split(src + jb.x + ps, la, src + jb.x + ps + la, lb, o - ps);
-      if (lane == 0) {
+      const int64_t s =
+          group_merge_split<16>(src + jb.x + ps, la, src + jb.x + ps + la, lb, o - ps);
+      if (gl == 0) {
         split[i] = static_cast<uint32_t>(s);
         desc[2 * i] = make_int4(static_cast<int32_t>(jb.x + ps), static_cast<int32_t>(la),
                                 static_cast<int32_t>(lb), static_cast<int32_t>(o - ps));
