@@ -382,24 +382,28 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
             int ai = lo, bi = dt - lo;
             K av = Xk[MS::xslot(ai < wa ? ai : 0)];
             K bv = Xk[MS::xslot(bi < wb ? wa + bi : 0)];
+            auto step = [&](int pos) {
+              const bool take_a =
+                  ai < wa && (bi >= wb || Ord::to_bits(av) <= Ord::to_bits(bv));
+              const int x = take_a ? ai : wa + bi;
+              Ok[MS::oslot(pos)] = take_a ? av : bv;
+              if constexpr (PAIRS) Ov[MS::oslot(pos)] = Xv[MS::xslot(x)];
+              ai += take_a;
+              bi += !take_a;
+              // Next head of the side just consumed (any in-range slot when
+              // that side is exhausted: it is never compared again).
+              const int nx = take_a ? (ai < wa ? ai : 0) : (bi < wb ? wa + bi : 0);
+              const K nv = Xk[MS::xslot(nx)];
+              av = take_a ? nv : av;
+              bv = take_a ? bv : nv;
+            };
+            if (dt + KPT <= m) {
 #pragma unroll
-            for (int q = 0; q < KPT; ++q) {
-              const int pos = dt + q;
-              if (pos < m) {
-                const bool take_a =
-                    ai < wa && (bi >= wb || Ord::to_bits(av) <= Ord::to_bits(bv));
-                const int x = take_a ? ai : wa + bi;
-                Ok[MS::oslot(pos)] = take_a ? av : bv;
-                if constexpr (PAIRS) Ov[MS::oslot(pos)] = Xv[MS::xslot(x)];
-                ai += take_a;
-                bi += !take_a;
-                // Next head of the side just consumed (any in-range slot when
-                // that side is exhausted: it is never compared again).
-                const int nx = take_a ? (ai < wa ? ai : 0) : (bi < wb ? wa + bi : 0);
-                const K nv = Xk[MS::xslot(nx)];
-                av = take_a ? nv : av;
-                bv = take_a ? bv : nv;
-              }
+              for (int q = 0; q < KPT; ++q) step(dt + q);
+            } else {
+#pragma unroll
+              for (int q = 0; q < KPT; ++q)
+                if (dt + q < m) step(dt + q);
             }
           }
           if (tid == 0 && more) publish(c ^ 1);

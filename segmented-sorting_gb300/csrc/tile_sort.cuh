@@ -849,19 +849,27 @@ __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsign
     int bi = a_end + diag - l;
     Word av = ai < a_end ? W[Cfg::wslot(ai)] : WT::maxv();
     Word bv = bi < hi_p ? W[Cfg::wslot(bi)] : WT::maxv();
+    auto step = [&](Word &out) {
+      const bool take_a = WT::le(av, bv);
+      out = take_a ? av : bv;
+      ai += take_a;
+      bi += !take_a;
+      const int nx = take_a ? ai : bi;
+      const int lim = take_a ? a_end : hi_p;
+      const Word nv = nx < lim ? W[Cfg::wslot(nx)] : WT::maxv();
+      av = take_a ? nv : av;
+      bv = take_a ? bv : nv;
+    };
+    if (base >= lo_p && base + KPT <= hi_p) {
+      // Every position of this thread is in the merge (always, for a chunk
+      // of one segment): no per-position check.
 #pragma unroll
-    for (int j = 0; j < KPT; ++j) {
-      const int p = base + j;
-      if (p >= lo_p && p < hi_p) {
-        const bool take_a = WT::le(av, bv);
-        w[j] = take_a ? av : bv;
-        ai += take_a;
-        bi += !take_a;
-        const int nx = take_a ? ai : bi;
-        const int lim = take_a ? a_end : hi_p;
-        const Word nv = nx < lim ? W[Cfg::wslot(nx)] : WT::maxv();
-        av = take_a ? nv : av;
-        bv = take_a ? bv : nv;
+      for (int j = 0; j < KPT; ++j) step(w[j]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < KPT; ++j) {
+        const int p = base + j;
+        if (p >= lo_p && p < hi_p) step(w[j]);
       }
     }
   }
