@@ -397,7 +397,25 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
               av = take_a ? nv : av;
               bv = take_a ? bv : nv;
             };
-            if (dt + KPT <= m) {
+            if (__all_sync(__activemask(), dt + KPT <= m && ai + KPT < wa && bi + KPT < wb)) {
+              // For every thread of the warp: neither window can run out
+              // within its KPT outputs, so no end-of-window tests (the last
+              // look-ahead reads at most element wa - 1 or m - 1).  Decided
+              // per warp, so warps do not diverge.
+#pragma unroll
+              for (int q = 0; q < KPT; ++q) {
+                const int pos = dt + q;
+                const bool take_a = Ord::to_bits(av) <= Ord::to_bits(bv);
+                const int x = take_a ? ai : wa + bi;
+                Ok[MS::oslot(pos)] = take_a ? av : bv;
+                if constexpr (PAIRS) Ov[MS::oslot(pos)] = Xv[MS::xslot(x)];
+                ai += take_a;
+                bi += !take_a;
+                const K nv = Xk[MS::xslot(take_a ? ai : wa + bi)];
+                av = take_a ? nv : av;
+                bv = take_a ? bv : nv;
+              }
+            } else if (dt + KPT <= m) {
 #pragma unroll
               for (int q = 0; q < KPT; ++q) step(dt + q);
             } else {
