@@ -22,7 +22,7 @@
 // because the segment start is the most significant field.  Segment starts
 // come from a shared-memory bitmask of segment heads and a block-wide running
 // maximum.  The sort is a merge sort: each thread sorts KPT words in registers
-// with a bitonic network, then log2(chunk / KPT) merge-path levels merge pairs
+// with a sorting network, then log2(chunk / KPT) merge-path levels merge pairs
 // of runs through shared memory.  A pair whose runs are already in order (last
 // word of the first run <= first word of the second) is left as it is, so
 // chunks of short aligned segments skip the upper levels.  Values are staged
@@ -221,10 +221,10 @@ __device__ __forceinline__ void transposition_sort(typename WT::T (&w)[KPT], int
 }
 
 // Longest segment (in words) for which the transposition rounds cost fewer
-// exchanges than the bitonic network: about KPT/2 - 1/2 exchanges a round
-// against KPT/2 * log2(KPT) * (log2(KPT) + 1) / 2 for the network.
+// exchanges than the sorting network: about KPT/2 - 1/2 exchanges a round
+// against 63 (16 words) or 19 (8 words) for Batcher's network.
 template <int KPT>
-constexpr int kTranspositionMaxRounds = KPT >= 16 ? 10 : (KPT >= 8 ? 6 : 2);
+constexpr int kTranspositionMaxRounds = KPT >= 16 ? 8 : (KPT >= 8 ? 5 : 2);
 
 // ---------------------------------------------------------------------------
 // Range copies between global memory and per-element callbacks: 16-byte
@@ -753,7 +753,7 @@ __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsign
   // Without merge levels no segment crosses a thread's block, and R rounds of
   // odd-even transposition sort every segment of at most R words (words of
   // different segments are already in order, so no exchange crosses a
-  // segment's boundary): cheaper than the bitonic network for short ones.
+  // segment's boundary): cheaper than the sorting network for short ones.
   int rounds = KPT;
   if (kShort && levels == 0) {
     const int lim = base < m ? min(KPT, m - base) : 0;
