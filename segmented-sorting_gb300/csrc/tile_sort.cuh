@@ -778,16 +778,24 @@ __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsign
   }
 
   // ---- merge levels ---------------------------------------------------------------
+  // A level whose pairs of runs span at most one warp (2 * run <= 32 * KPT)
+  // reads and writes only its own warp's part of W, so a warp barrier
+  // orders it; a level whose pairs span several warps needs block barriers,
+  // and so does the level after it (its readers crossed warps).  Before the
+  // first level every thread has read only its own words.
   bool dirty = true;  // W does not hold this thread's current words
+  bool prev_local = true;
   int level = 0;
   for (int run = KPT; run < m && level < levels; run <<= 1, ++level) {
-    __syncthreads();  // previous readers of W are done
+    const int pair_threads = (2 * run) / KPT;
+    const bool local = pair_threads <= 32;
+    if (prev_local) __syncwarp(); else __syncthreads();  // previous readers of W are done
     if (dirty) {
 #pragma unroll
       for (int j = 0; j < KPT; ++j) W[Cfg::wslot(base + j)] = w[j];
     }
-    __syncthreads();
-    const int pair_threads = (2 * run) / KPT;
+    if (local) __syncwarp(); else __syncthreads();
+    prev_local = local;
     const int r = tid & (pair_threads - 1);
     const int a_beg = (tid - r) * KPT;
     const int a_end = a_beg + run;
