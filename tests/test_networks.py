@@ -1,0 +1,128 @@
+"""CPU checks of the combinatorial facts the sort kernels rely on.
+
+* Batcher's odd-even merge network, enumerated by the same loop nest as
+  BatcherNet<N>::pair (segmented-sorting_gb300/csrc/tile_sort.cuh), sorts
+  every 0-1 input of 4, 8 and 16 words (so every input, by the 0-1
+  principle) with 5, 19 and 63 compare-exchanges, each (low, high).
+* R rounds of odd-even transposition sort any run of at most R words,
+  whichever parity the run's first position has (transposition_sort).
+* The half-tile classify (one lower-bound search per half-tile entry and one
+  long-segment candidate per half-tile, large_classify_halves_kernel in
+  csrc/classify.cuh) writes the same half-tile map and job list as the
+  per-boundary classify (classify_boundary).
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+import pytest
+
+
+def batcher_pairs(n: int) -> list[tuple[int, int]]:
+    out = []
+    p = 1
+    while p < n:
+        k = p
+        while k >= 1:
+            j = k % p
+            while j + k < n:
+                for i in range(min(k, n - j - k)):
+                    if (i + j) // (2 * p) == (i + j + k) // (2 * p):
+                        out.append((i + j, i + j + k))
+                j += 2 * k
+            k //= 2
+        p *= 2
+    return out
+
+
+def zero_one_inputs(n: int) -> np.ndarray:
+    return np.array(list(itertools.product([0, 1], repeat=n)), dtype=np.int8)
+
+
+@pytest.mark.parametrize("n,size", [(4, 5), (8, 19), (16, 63)])
+def test_batcher_network_sorts_every_input(n, size):
+    pairs = batcher_pairs(n)
+    assert len(pairs) == size and all(a < b for a, b in pairs)
+    x = zero_one_inputs(n)
+    for a, b in pairs:
+        lo = np.minimum(x[:, a], x[:, b])
+        hi = np.maximum(x[:, a], x[:, b])
+        x[:, a], x[:, b] = lo, hi
+    assert np.all(np.diff(x, axis=1) >= 0)
+
+
+@pytest.mark.parametrize("length", list(range(1, 17)))
+def test_transposition_rounds_sort_runs_of_their_length(length):
+    x0 = zero_one_inputs(length)
+    for parity in (0, 1):
+        x = x0.copy()
+        for r in range(length):
+            for i in range((r + parity) % 2, length - 1, 2):
+                lo = np.minimum(x[:, i], x[:, i + 1])
+                hi = np.maximum(x[:, i], x[:, i + 1])
+                x[:, i], x[:, i + 1] = lo, hi
+        assert np.all(np.diff(x, axis=1) >= 0), (length, parity)
+
+
+def _off(o, nseg, i, n):
+    return min(max(int(o[i]), 0), n)
+
+
+def _lower_bound(o, nseg, n, x):
+    """The warp's 32-ary search of warp_lower_bound, one probe set per round."""
+    lo, hi = 0, nseg
+    while hi > lo:
+        span = hi - lo
+        small = span <= 32
+        probes = [lo + l if small else lo + (span * (l + 1)) // 33 for l in range(32)]
+        ge = [True if (small and l >= span) else _off(o, nseg, probes[l], n) >= x
+              for l in range(32)]
+        c = sum(1 for g in ge if not g)
+        assert ge == [False] * c + [True] * (32 - c)  # a monotone ballot
+        if small:
+            lo += c
+            hi = lo
+        else:
+            lo, hi = (probes[c - 1] + 1 if c > 0 else lo), (probes[c] if c < 32 else hi)
+    return lo
+
+
+def test_half_tile_classify_matches_per_boundary_classify():
+    rng = np.random.default_rng(0)
+    cap, half = 4096, 2048
+    for trial in range(48):
+        nseg = int(rng.integers(1, 2500))
+        kind = trial % 4
+        if kind == 0:
+            lens = rng.integers(0, 5, nseg)
+        elif kind == 1:
+            lens = rng.integers(0, 9000, nseg) * (rng.random(nseg) < 0.3)
+        elif kind == 2:
+            lens = np.where(rng.random(nseg) < 0.01, rng.integers(4097, 20000, nseg),
+                            rng.integers(0, 3, nseg))
+        else:
+            lens = rng.integers(1, 100, nseg)
+        o = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+        n = int(o[-1]) + int(rng.integers(0, 50))
+        halves = 2 * max(1, (n + cap - 1) // cap)
+        # per-boundary definition: boundary s owns the entries h with
+        # off(s-1) < h*half <= off(s) (off(-1) = -inf, off(nseg) = +inf)
+        ref = [None] * (halves + 1)
+        for s in range(nseg + 1):
+            cur = _off(o, nseg, s, n) if s < nseg else 0
+            h_lo = 0 if s == 0 else _off(o, nseg, s - 1, n) // half + 1
+            h_hi = halves if s == nseg else min(cur // half, halves)
+            for h in range(h_lo, h_hi + 1):
+                ref[h] = s
+        jobs_ref = sorted((_off(o, nseg, s, n), _off(o, nseg, s + 1, n)) for s in range(nseg)
+                          if _off(o, nseg, s + 1, n) - _off(o, nseg, s, n) > cap)
+        hf = [_lower_bound(o, nseg, n, h * half) for h in range(halves + 1)]
+        assert hf == ref, trial
+        jobs = []
+        for h in range(halves):
+            if hf[h + 1] > hf[h]:
+                beg, end = _off(o, nseg, hf[h + 1] - 1, n), _off(o, nseg, hf[h + 1], n)
+                if end - beg > cap:
+                    jobs.append((beg, end))
+        assert sorted(jobs) == jobs_ref, trial
