@@ -168,6 +168,31 @@ def test_key_types(pkg, cuda, oracle, inst, dtype):
     check_both(pkg, cuda, oracle, keys, off)
 
 
+@pytest.mark.parametrize("dtype", [np.int32, np.float32, np.uint64])
+def test_short_segment_key_types(pkg, cuda, oracle, inst, dtype):
+    """Every key type on problems of short ragged segments (average below 32,
+    over many tiles: the streamed tile kernel and the half-tile classify),
+    with a few long segments among them."""
+    rng = np.random.default_rng(31)
+    lens = rng.integers(0, 20, 6000)
+    lens[::1500] = [5000, 9000, 4097, 12000]
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    n = int(off[-1])
+    assert n < 32 * (len(off) - 1)
+    if dtype == np.float32:
+        keys = (rng.standard_normal(n) * 10).astype(np.float32)
+        specials = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-42, -1e-42], np.float32)
+        keys[rng.integers(0, n, 500)] = specials[rng.integers(0, len(specials), 500)]
+    elif dtype == np.int32:
+        keys = inst.uniform_keys(n, seed=32, bits=6).astype(np.int32) - 32
+        keys[::13] = np.int32(-2147483648)
+        keys[::17] = 2147483647
+    else:
+        keys = inst.uniform_keys(n, seed=33, bits=64, dtype=np.uint64)
+        keys[::3] &= np.uint64(0xFF)
+    check_both(pkg, cuda, oracle, keys, off)
+
+
 def test_heads_only_offsets(pkg, cuda, oracle, inst):
     n = 60000
     csr = inst.diff_offsets(n, 50, seed=11)
