@@ -354,8 +354,9 @@ def bench_served(requests: int, rates: str) -> dict:
 
 def bench_configs(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
     """The plain call on the other single-instance workloads: 2^20 keys-only
-    (1024 x 1024, keys < 2^31) and 2^25 pairs with lognormal segment lengths
-    (uniform and Zipf(1.1) keys)."""
+    (1024 x 1024, keys < 2^31), 2^25 pairs with lognormal segment lengths
+    (uniform and Zipf(1.1) keys), and the equal-segment sweep's low-entropy
+    variant (2^24 pairs, keys in [0, 16), segment lengths 2^1..2^20)."""
     import torch
     L = pkg.lib()
     st = stream.cuda_stream
@@ -389,6 +390,27 @@ def bench_configs(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
             "ms": round(ms, 4), "gkeys_s": round(n3 / (ms * 1e-3) / 1e9, 3),
             "segments": int(len(lens)), "empty": int((lens == 0).sum()),
             "max_len": int(lens.max())}
+    n2 = 1 << 24
+    k4 = inst.device_uniform_keys(n2, seed=16, bits=4, device=dev)
+    v2 = torch.arange(n2, dtype=torch.int32, device=dev)
+    kk, vv = torch.empty_like(k4), torch.empty_like(v2)
+
+    def restore4():
+        kk.copy_(k4)
+        vv.copy_(v2)
+
+    per = {}
+    total_ms = 0.0
+    for lg in range(1, 21):
+        o2 = torch.from_numpy(inst.equal_offsets(n2, 1 << lg)).to(dev)
+        t = _timed(stream, lambda: L.segsort_pairs_u32(kk.data_ptr(), vv.data_ptr(), n2,
+                                                       o2.data_ptr(), o2.numel() - 1, st),
+                   restore4, warmup, steps)
+        ms = statistics.median(t)
+        per[lg] = round(ms, 4)
+        total_ms += ms
+    out["pairs_2e24_keys_0_16_sweep"] = {
+        "ms_per_len": per, "gkeys_s": round(20 * n2 / (total_ms * 1e-3) / 1e9, 3)}
     if pkg.device_status() != 0:
         raise RuntimeError("device status reports a bounded wait that gave up")
     return out
