@@ -10,6 +10,10 @@
   long-segment candidate per half-tile, large_classify_halves_kernel in
   csrc/classify.cuh) writes the same half-tile map and job list as the
   per-boundary classify (classify_boundary).
+* The streamed tile kernel's staging geometry (StagedSpan in
+  csrc/tile_stream.cuh): the bulk copy starts on a 16-byte boundary inside
+  the range's first granule, covers every element, and stays inside the
+  staging buffer (CAP + 32 / sizeof(T) elements, CAP/2 + 8 for offsets).
 """
 from __future__ import annotations
 
@@ -126,3 +130,21 @@ def test_half_tile_classify_matches_per_boundary_classify():
                 if end - beg > cap:
                     jobs.append((beg, end))
         assert sorted(jobs) == jobs_ref, trial
+
+
+@pytest.mark.parametrize("elem", [4, 8])
+def test_staged_span_geometry(elem):
+    cap = 4096 if elem == 4 else 2048
+    v = 16 // elem
+    for stage_cap, limit in ((cap + 32 // elem, cap), (cap // 2 + 8, cap // 2)):
+        for addr_elems in range(0, 2 * v):       # the range's first element, in elements
+            for m in list(range(1, 40)) + [limit - 1, limit]:
+                byte0 = addr_elems * elem
+                mis = (byte0 & 15) // elem
+                nvec = (mis + m + v - 1) // v
+                copy_from = byte0 - mis * elem   # the bulk copy's global start
+                assert copy_from % 16 == 0 and copy_from >= (byte0 // 16) * 16
+                assert mis + m <= nvec * v       # every element is copied
+                assert nvec * v <= stage_cap     # inside the staging buffer
+                # the last granule holds the range's last element (no granule past it)
+                assert (copy_from + 16 * nvec) - (byte0 + m * elem) < 16
