@@ -9,10 +9,11 @@
 // the half-tile's end, so nothing else starts after it there), so the short
 // segments of a half-tile span less than CAP elements and form one chunk; the
 // two halves' chunks are joined when they are contiguous and fit together.
-// A last segment longer than CAP/2 is a chunk of its own (up to CAP) or is
-// left to the large-segment path (longer than CAP).  A CTA therefore sorts at
-// most four chunks, found from three half_first entries and five offsets,
-// without any search.
+// A last segment longer than CAP/2 is a chunk of its own (up to CAP) or, when
+// longer than CAP, a long segment whose first CAP-run the CTA sorts for the
+// merge passes.  With the CAP-run of a long segment that started before the
+// tile, a CTA sorts at most five chunks (kMaxTileChunks), found from three
+// half_first entries and a few offsets, without any search.
 //
 // Chunk sort.  Every element becomes a composite word
 //     (segment start within the chunk, order bits of the key, chunk index)
