@@ -12,18 +12,24 @@ Printed JSON line (rank 0):
   value       Gkeys/s over the K timed steps, inputs resident in HBM
   e2e         the same through the Python API with pinned host buffers:
               host->device copy of keys+values, sort, device->host copy,
-              on two streams so that one instance's copies overlap the
-              other's sort
-  roofline    the dominant kernel phase, algorithmic bytes (read and write
-              every key and value once, plus the offsets) / its CUDA-event
-              time measured live on the launching stream, against the
-              measured HBM copy bandwidth
+              four instances in flight on four streams; every instance read
+              back is checked (sorted within segments, keys moved with their
+              values)
+  roofline    the dominant kernel, algorithmic bytes (read and write every
+              key and value once per pass over them, plus the offsets or the
+              radix digit counts) / its CUDA-event time measured live on the
+              launching stream, against the measured HBM copy bandwidth
   cpu_baseline  the oracle's per-segment std::stable_sort (the reference's
-              CPU algorithm, src/mseq.cu:44-49) on all host threads, on a
-              2^22-key sample of every instance
+              CPU algorithm, src/mseq.cu:44-49) on the same full instances:
+              one step on all host threads and one on a single thread (the
+              reference's mseq is sequential)
   per_len     per segment length: ms, Gkeys/s and fraction of the HBM roofline
+  batched, served, configs   the other workloads (64-instance batch, Poisson
+              request stream, 2^20 keys-only, 2^25 lognormal, low entropy)
 
---impl reference times that CPU algorithm as the reference arm (rank 0).
+--impl reference times that CPU algorithm as the reference arm (rank 0), on
+the same instances and the same config.  --served-only runs the request
+stream alone (e.g. the full 1k..50k req/s sweep).
 """
 from __future__ import annotations
 
@@ -50,7 +56,6 @@ METRIC = "segsort Gkeys/s vs segment size, % HBM roofline; batched/served p50/p9
 WORKLOAD = ("equal-segment sweep: 2^24 uint32 key/value pairs per instance, keys uniform "
             "in [0,2^32), values = index, segment length 2^1..2^20 (one instance each)")
 BYTES_PER_PAIR = 16  # read key+value once, write key+value once
-STREAM_MAX_AVG = 32  # the library's streamed-tile threshold (segsort_api.cu)
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -63,14 +68,15 @@ def parse_args():
     p.add_argument("--log-n", type=int, default=24)
     p.add_argument("--lengths", type=str, default="1-20",
                    help="log2 segment lengths, e.g. 1-20 or 4,8,12")
-    p.add_argument("--cpu-sample-log", type=int, default=22)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the 64-instance batch")
     p.add_argument("--no-configs", action="store_true", help="skip the other workloads")
     p.add_argument("--no-served", action="store_true", help="skip the served-form stream")
-    p.add_argument("--served-requests", type=int, default=1000)
-    p.add_argument("--served-rates", type=str, default="1000,10000,50000")
+    p.add_argument("--served-requests", type=int, default=100000)
+    p.add_argument("--served-rates", type=str, default="10000,20000,50000")
+    p.add_argument("--served-only", action="store_true",
+                   help="run only the served-form request stream and print its JSON")
     return p.parse_args()
 
 
@@ -160,31 +166,66 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def cpu_sort_sample(O, inst, n_sample: int, lengths: list[int], threads: int) -> tuple[float, int]:
-    """Seconds to sort, with the oracle's std::stable_sort per segment on
-    `threads` threads, the first n_sample pairs of every instance."""
-    total = 0.0
-    keys_done = 0
-    for lg in lengths:
-        ln = 1 << lg
-        m = max(n_sample // ln, 1) * ln
-        keys = inst.uniform_keys(m, seed=1000 + lg, bits=32)
-        off = inst.equal_offsets(m, ln)
-        vals = np.arange(m, dtype=np.uint32)
-        k = keys.copy()
-        v = vals.copy()
-        kp = k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
-        vp = v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
-        op = off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
-        t0 = time.perf_counter()
-        O.lib().oracle_segsort_pairs_u32(kp, vp, m, op, len(off) - 1, threads)
-        total += time.perf_counter() - t0
-        keys_done += m
-    return total, keys_done
+def bench_config(n: int, lengths: list[int], world: int) -> dict:
+    """The workload's config, identical for both arms."""
+    return {"workload": WORKLOAD, "n": n, "log2_lengths": lengths,
+            "l2": "inputs larger than L2: 128 MiB fresh instance per call",
+            "parallelism": f"replicas{world}"}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+class CpuSweep:
+    """The sweep's instances in host memory (the same keys the GPU arm
+    sorts), sorted by the oracle's std::stable_sort per segment -- the
+    reference's mseq algorithm -- on fresh copies every step."""
+
+    def __init__(self, O, inst, n: int, lengths: list[int]):
+        self.O, self.n = O, n
+        self.items = [(inst.uniform_keys(n, seed=1000 + lg, bits=32), inst.equal_offsets(n, 1 << lg))
+                      for lg in lengths]
+        self.vals = np.arange(n, dtype=np.uint32)
+        self.k = np.empty(n, np.uint32)
+        self.v = np.empty(n, np.uint32)
+
+    def step(self, threads: int) -> float:
+        """Seconds spent sorting (copies outside)."""
+        total = 0.0
+        kp = self.k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        vp = self.v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        for keys, off in self.items:
+            np.copyto(self.k, keys)
+            np.copyto(self.v, self.vals)
+            op = off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            t0 = time.perf_counter()
+            self.O.lib().oracle_segsort_pairs_u32(kp, vp, self.n, op, len(off) - 1, threads)
+            total += time.perf_counter() - t0
+        return total
+
+    @property
+    def keys_per_step(self) -> int:
+        return self.n * len(self.items)
 
 
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     from oracle import oracle as O
@@ -192,27 +233,23 @@ def run_reference(args) -> None:
     entry.load_package()
     inst = importlib.import_module(f"{entry.PKG_NAME}.instances")
     lengths = log_lengths(args.lengths)
+    n = 1 << args.log_n
     threads = O.default_threads()
-    n_sample = 1 << min(args.cpu_sample_log, args.log_n)
+    sweep = CpuSweep(O, inst, n, lengths)
     for _ in range(args.warmup):
-        cpu_sort_sample(O, inst, n_sample, lengths, threads)
-    secs, keys = 0.0, 0
-    for _ in range(args.steps):
-        s, k = cpu_sort_sample(O, inst, n_sample, lengths, threads)
-        secs += s
-        keys += k
-    value = keys / secs / 1e9
-    sample = (f"first {n_sample} pairs (whole segments) of each of the {len(lengths)} "
-              f"instances per step")
+        sweep.step(threads)
+    secs = sum(sweep.step(threads) for _ in range(args.steps))
+    value = sweep.keys_per_step * args.steps / secs / 1e9
+    sample = (f"the full sweep every step: {len(lengths)} instances of {n} pairs, "
+              f"std::stable_sort per segment on {threads} threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gkeys/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": 1 << args.log_n,
-                   "log2_lengths": lengths, "l2": "inputs larger than L2 (CPU arm)"},
+        "config": bench_config(n, lengths, world),
         "cpu_baseline": {"value": value, "unit": "Gkeys/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "cpu_model": cpu_model(), "sample": sample},
         "e2e": {"value": value, "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -343,13 +380,14 @@ def bench_served(requests: int, rates: str) -> dict:
     exe = entry.PKG_DIR / "serve_bench.exe"
     cmd = [str(exe), "--requests", str(requests), "--rates", rates, "--budget-gb", "64",
            "--seed", "7"]
-    r = subprocess.run(cmd, capture_output=True, text=True, timeout=1200)
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=3600)
     if r.returncode != 0:
         raise RuntimeError(f"serve_bench failed ({r.returncode}): {r.stderr[-2000:]}")
     rows = [json.loads(line) for line in r.stdout.splitlines() if line.strip()]
     return {"workload": SERVED_WORKLOAD,
-            "sample": f"{requests} requests per rate (the same requests at every rate)",
-            "rates": rows}
+            "sample": f"{requests} requests per rate (the same requests at every rate), "
+                      f"rates {rates} req/s",
+            "requests": requests, "rates": rows}
 
 
 def bench_configs(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
@@ -519,9 +557,9 @@ def run_ours(args) -> None:
         torch.cuda.synchronize()
         phase[lg] = pkg.profile_read(reset=True)
     pkg.profile_enable(False)
-    cap = 4096  # tile capacity of 32-bit keys: longer segments take the merge passes
-    tile_ms = sum(p["tile_ms"] for p in phase.values())
-    large_ms = sum(p["large_ms"] for p in phase.values())
+    cap = 4096  # tile capacity of 32-bit keys: longer segments take a long-segment route
+    radix_min = pkg.get_param(pkg.PARAM_RADIX_MIN_32)
+    stream_max_avg = pkg.get_param(pkg.PARAM_STREAM_MAX_AVG)
     launches_per_step = sum(p["tile_launches"] + p["large_launches"] for p in phase.values())
 
     def merge_passes(length: int) -> int:
@@ -530,28 +568,62 @@ def run_ours(args) -> None:
             runs, p = (runs + 1) // 2, p + 1
         return p
 
+    def varying_digits(lg: int) -> int:
+        """8-bit digit positions whose value differs somewhere inside a
+        segment of the instance: the radix passes the library runs."""
+        k = pristine[lg].long() & 0xFFFFFFFF
+        seg = torch.arange(n, device=dev) >> lg
+        count = 0
+        for d in range(4):
+            dg = (k >> (8 * d)) & 255
+            lo = torch.full((n >> lg,), 256, dtype=torch.long, device=dev).scatter_reduce(
+                0, seg, dg, reduce="amin")
+            hi = torch.full((n >> lg,), -1, dtype=torch.long, device=dev).scatter_reduce(
+                0, seg, dg, reduce="amax")
+            count += int(bool((lo != hi).any()))
+        return count
+
     # Algorithmic bytes per launch.  The tile kernel reads and writes every
-    # key and value once in every call (it sorts the short segments and forms
-    # the sorted runs of the long ones) and reads the offsets; each merge pass
-    # reads and writes every key and value of the long segments once.
-    # The library runs the streamed tile kernel when the average segment is at
-    # most STREAM_MAX_AVG long, the one-CTA-per-tile kernel otherwise.
-    tile_bytes = {lg: BYTES_PER_PAIR * n + 4 * (n // (1 << lg) + 1) for lg in lengths}
-    stream_bytes = {lg: b for lg, b in tile_bytes.items() if (1 << lg) <= STREAM_MAX_AVG}
-    plain_bytes = {lg: b for lg, b in tile_bytes.items() if (1 << lg) > STREAM_MAX_AVG}
-    merge_bytes = {lg: BYTES_PER_PAIR * n * merge_passes(1 << lg) for lg in lengths
-                   if (1 << lg) > cap}
+    # key and value once and reads the offsets: all of them when the segments
+    # are at most a tile long, the long segments' elements when it forms their
+    # sorted runs for the merge passes.  A merge pass reads and writes every key
+    # and value of its segments once.  The radix route reads every key once
+    # for the digit counts, then reads and writes every key and value once per
+    # digit position that varies, plus one copy back after an odd number of
+    # passes.  The library runs the streamed tile kernel when the average
+    # segment is at most stream_max_avg long, the one-CTA-per-tile kernel
+    # otherwise.
+    tile_bytes, stream_bytes, long_bytes, idle_tile = {}, {}, {}, []
+    for lg in lengths:
+        ln = 1 << lg
+        full = BYTES_PER_PAIR * n + 4 * (n // ln + 1)
+        if ln <= stream_max_avg:
+            stream_bytes[lg] = full
+        elif ln <= cap:
+            tile_bytes[lg] = full
+        elif ln <= radix_min:
+            tile_bytes[lg] = full
+            long_bytes[lg] = BYTES_PER_PAIR * n * merge_passes(ln)
+        else:
+            idle_tile.append(lg)  # the tile kernel finds no work: every segment is on the radix route
+            passes = varying_digits(lg)
+            long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n * (passes + (passes & 1))
     kernels = {}
-    for name, table, key in (("tile_sort_kernel", plain_bytes, "tile_ms"),
+    for name, table, key in (("tile_sort_kernel", tile_bytes, "tile_ms"),
                              ("tile_stream_kernel", stream_bytes, "tile_ms"),
-                             ("merge_sort_kernel", merge_bytes, "large_ms")):
+                             ("long_segment_kernel", long_bytes, "large_ms")):
         ms_sum = sum(phase[lg][key] for lg in table)
         byts = sum(table.values())
         if ms_sum > 0 and table:
             kernels[name] = {"ms_per_step": round(ms_sum, 4), "launches_per_step": len(table),
                              "algorithmic_bytes_per_step": byts,
                              "achieved_gbs": round(byts / (ms_sum * 1e-3) / 1e9, 1)}
-    name = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
+    if idle_tile:
+        kernels["tile_sort_kernel_no_work"] = {
+            "ms_per_step": round(sum(phase[lg]["tile_ms"] for lg in idle_tile), 4),
+            "launches_per_step": len(idle_tile), "algorithmic_bytes_per_step": 0}
+    name = max((k for k in kernels if kernels[k].get("algorithmic_bytes_per_step")),
+               key=lambda k: kernels[k]["ms_per_step"])
     K = kernels[name]
     achieved = K["achieved_gbs"]
     tr = traffic_per_launch()
@@ -561,6 +633,7 @@ def run_ours(args) -> None:
                 "algorithmic_bytes_per_launch": K["algorithmic_bytes_per_step"] // K["launches_per_step"],
                 "traffic": ((tr or {}).get(name) or {}).get("dram_bytes_per_launch"),
                 "traffic_workload": ((tr or {}).get(name) or {}).get("workload"),
+                "radix_min": radix_min, "stream_max_avg": stream_max_avg,
                 "kernels": kernels}
 
     # ---- end to end through the public API with host buffers ---------------
@@ -621,15 +694,23 @@ def run_ours(args) -> None:
                "h2d_bytes_per_step": 8 * n * len(lengths),
                "d2h_bytes_per_step": 8 * n * len(lengths),
                "steps": e_steps, "ms_per_step": e_ms / e_steps}
-        # the host copies read back hold sorted segments with their values
-        lg = lengths[-1]
-        hk, hv, ok, ov = host[lg]
-        seg = min(1 << lg, n)
-        got_k = ok[:seg].numpy().view(np.uint32)
-        got_v = ov[:seg].numpy().view(np.uint32)
-        src_k = hk[:seg].numpy().view(np.uint32)
-        if not (np.all(got_k[:-1] <= got_k[1:]) and np.array_equal(src_k[got_v], got_k)):
-            raise RuntimeError("end-to-end read-back is not the sorted segment")
+        # Every instance read back into host memory holds its stable sort:
+        # within each segment the values are a permutation of the segment's
+        # positions, the keys moved with them, in order, ties in input order.
+        for lg in lengths:
+            hk, hv, ok, ov = host[lg]
+            k = ok.to(dev).long() & 0xFFFFFFFF
+            v = ov.to(dev).long() & 0xFFFFFFFF
+            src = hk.to(dev).long() & 0xFFFFFFFF
+            pos = torch.arange(n, device=dev)
+            same = (pos[1:] >> lg) == (pos[:-1] >> lg)
+            ok_all = (bool(((v >> lg) == (pos >> lg)).all())
+                      and bool((torch.bincount(v, minlength=n) == 1).all())
+                      and torch.equal(src[v], k)
+                      and bool(((k[1:] > k[:-1]) | ~same | ((k[1:] == k[:-1]) & (v[1:] > v[:-1]))).all()))
+            if not ok_all:
+                raise RuntimeError(f"end-to-end read-back of segment length 2^{lg} is not its stable sort")
+        e2e["checked"] = f"every instance read back ({len(lengths)} x {n} pairs)"
 
     # ---- the batched form and the other workloads ---------------------------
     batched = None if args.no_batched else bench_batched(pkg, inst, dev, stream, 2, 5)
@@ -638,18 +719,24 @@ def run_ours(args) -> None:
     if rank == 0 and not args.no_served:
         served = bench_served(args.served_requests, args.served_rates)
 
-    # ---- CPU baseline (rank 0) ----------------------------------------------
+    # ---- CPU baseline (rank 0): the same full instances, all host threads and
+    # one thread -------------------------------------------------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         O.build()
         threads = O.default_threads()
-        n_sample = 1 << min(args.cpu_sample_log, args.log_n)
-        secs, keys = cpu_sort_sample(O, inst, n_sample, lengths, threads)
-        cpu = {"value": keys / secs / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
-               "sample": f"first {n_sample} pairs (whole segments) of each instance, "
-                         f"{len(lengths)} instances, std::stable_sort per segment on "
-                         f"{threads} threads"}
+        sweep = CpuSweep(O, inst, n, lengths)
+        secs = sweep.step(threads)
+        secs1 = sweep.step(1)
+        cpu = {"value": sweep.keys_per_step / secs / 1e9, "unit": "Gkeys/s", "cores": threads,
+               "kind": "port", "cpu_model": cpu_model(),
+               "sample": f"one step of the full sweep ({len(lengths)} instances of {n} pairs), "
+                         f"std::stable_sort per segment on {threads} threads",
+               "single_thread": {"value": sweep.keys_per_step / secs1 / 1e9, "unit": "Gkeys/s",
+                                 "cores": 1, "sample": "one step of the full sweep on 1 thread "
+                                                      "(the reference's mseq is sequential)"}}
+        del sweep
 
     if rank == 0:
         print(json.dumps({
@@ -657,9 +744,7 @@ def run_ours(args) -> None:
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": region_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": n, "log2_lengths": lengths,
-                       "l2": "inputs larger than L2: 128 MiB fresh instance per call",
-                       "parallelism": f"replicas{world}"},
+            "config": bench_config(n, lengths, world),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(), "per_len": per_len,
@@ -669,10 +754,18 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def run_served_only(args) -> None:
+    entry.load_package().build()
+    print(json.dumps({"metric": "served-form request stream (p50/p99/p999 ms, Gkeys/s)",
+                      "served": bench_served(args.served_requests, args.served_rates)}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.served_only:
+        run_served_only(args)
     else:
         run_ours(args)
 

@@ -143,7 +143,7 @@ int segsort_keys_u32_ws(uint32_t *d_keys, int64_t n, const int32_t *d_offsets,
  * or fail on, an allocation once running, and code that must not fail with
  * out-of-memory in mid-run.  The temporary storage is a fixed scratch array
  * that is part of the library's device code, sized for n up to
- * SEGSORT_NOALLOC_MAX_N uint32 key/value pairs (about 8 MiB); every GPU
+ * SEGSORT_NOALLOC_MAX_N uint32 key/value pairs (about 10 MiB); every GPU
  * that loads the library holds it until the process exits.  The call makes
  * no cudaMalloc, cudaFree or other allocating call.
  *
@@ -361,6 +361,41 @@ void segsort_server_destroy(segsort_server server);
 int segsort_device_status(int clear);
 const char *segsort_error_string(int code);
 int segsort_version(void);
+
+/* The library's own stream-ordered pool on the current device: *created = 1
+ * once the first call that allocates from it has created it (0 before), and
+ * *used = the bytes its allocations hold right now (cudaMemPoolAttrUsedMemCurrent;
+ * 0 when idle, since every call frees what it takes on its stream).  A
+ * diagnostic, e.g. to show that the allocation-free entry point never
+ * creates the pool.  No counterpart in the reference. */
+int segsort_pool_bytes(int *created, uint64_t *used);
+
+/* Run-time tuning parameters, process-wide (no counterpart in the reference,
+ * whose variants fix their thresholds at compile time, e.g. the bin bounds
+ * of src/bb_segsort/bb_bin.h:54-100).
+ *   SEGSORT_PARAM_RADIX_MIN_32 / _64: segments longer than this many keys
+ *     (32-bit / 64-bit keys) are sorted by LSD radix passes; shorter long
+ *     segments by merge passes over tile-sorted runs.  At least 4096.
+ *   SEGSORT_PARAM_STREAM_MAX_AVG: problems whose average segment (n / nseg)
+ *     is at most this long take the streamed short-segment tile kernel.
+ * A change applies to calls made after it; batch plans keep the values they
+ * were created with.  SEGSORT_ERR_INVALID_ARG for an unknown parameter or a
+ * value out of range. */
+#define SEGSORT_PARAM_RADIX_MIN_32 1
+#define SEGSORT_PARAM_RADIX_MIN_64 2
+#define SEGSORT_PARAM_STREAM_MAX_AVG 3
+int segsort_set_param(int param, int64_t value);
+int segsort_get_param(int param, int64_t *value);
+
+/* Self-test of the bounded device waits (no counterpart in the reference).
+ * Launches a small kernel on a stream of its own whose wait can never
+ * complete -- which = 0: a grid barrier that one of its two CTAs never
+ * reaches; 1: an mbarrier phase expecting bytes that no copy supplies; 2: a
+ * radix look-back on a tile that never publishes -- with a spin limit of a
+ * few milliseconds.  The kernel gives up, records SEGSORT_ERR_TIMEOUT for
+ * segsort_device_status() and returns; this call returns SEGSORT_OK once it
+ * has finished.  No GPU fault is involved. */
+int segsort_selftest_wait_timeout(int which);
 
 /* Phase timing for benchmarks.  While enabled, every sort call records CUDA
  * events on its own stream around its tile-sort kernel and around its

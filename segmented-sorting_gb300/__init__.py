@@ -30,6 +30,11 @@ SEGSORT_ERR_TOO_LARGE = -5
 SEGSORT_ERR_WORKSPACE = -6
 SEGSORT_NOALLOC_MAX_N = 1 << 20  # include/segsort.h
 
+# Run-time parameters (SEGSORT_PARAM_* of include/segsort.h).
+PARAM_RADIX_MIN_32 = 1
+PARAM_RADIX_MIN_64 = 2
+PARAM_STREAM_MAX_AVG = 3
+
 KEY_TYPES = ("u32", "i32", "f32", "u64")
 KEY_TYPE_CODES = {"u32": 0, "i32": 1, "f32": 2, "u64": 3}  # SEGSORT_KEY_* of include/segsort.h
 
@@ -83,6 +88,10 @@ SIGNATURES = {
     "segsort_server_drain": ([_P], ctypes.c_int),
     "segsort_server_get_stats": ([_P, ctypes.POINTER(ServerStats)], ctypes.c_int),
     "segsort_server_destroy": ([_P], None),
+    "segsort_pool_bytes": ([ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "segsort_set_param": ([ctypes.c_int, _I64], ctypes.c_int),
+    "segsort_get_param": ([ctypes.c_int, ctypes.POINTER(_I64)], ctypes.c_int),
+    "segsort_selftest_wait_timeout": ([ctypes.c_int], ctypes.c_int),
     "segsort_device_status": ([ctypes.c_int], ctypes.c_int),
     "segsort_error_string": ([ctypes.c_int], ctypes.c_char_p),
     "segsort_version": ([], ctypes.c_int),
@@ -200,6 +209,35 @@ def segsort(keys, offsets, values=None, *, key_type: str | None = None, heads: b
 def device_status(clear: bool = True) -> int:
     """Synchronise and return the device-side status (0 = no bounded wait gave up)."""
     return lib().segsort_device_status(1 if clear else 0)
+
+
+def get_param(param: int) -> int:
+    v = ctypes.c_int64()
+    _check(lib().segsort_get_param(param, ctypes.byref(v)), "segsort_get_param")
+    return v.value
+
+
+def set_param(param: int, value: int) -> None:
+    _check(lib().segsort_set_param(param, value), "segsort_set_param")
+
+
+class params:
+    """Context manager that sets run-time parameters and restores them:
+    `with params({PARAM_RADIX_MIN_32: 1 << 30}): ...`"""
+
+    def __init__(self, values: dict):
+        self._values = dict(values)
+        self._saved = {}
+
+    def __enter__(self):
+        for k, v in self._values.items():
+            self._saved[k] = get_param(k)
+            set_param(k, v)
+        return self
+
+    def __exit__(self, *exc):
+        for k, v in self._saved.items():
+            set_param(k, v)
 
 
 def workspace_bytes(n: int, nseg: int, key_bytes: int = 4, val_bytes: int = 4) -> int:

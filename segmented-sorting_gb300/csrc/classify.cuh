@@ -5,9 +5,10 @@
 // Classify replaces the reference's length binning bb_bin
 // (src/bb_segsort/bb_bin.h:23,31-139): instead of 13 power-of-two bins and a
 // device-to-host copy of their counts (bb_bin.h:46), it writes a half-tile ->
-// first-segment map that the tile sort reads directly, and a device-side list
-// of the segments longer than the tile capacity for the merge passes.  Two
-// forms write the same map and list: one thread per segment boundary
+// first-segment map that the tile sort reads directly, and two device-side
+// lists of the segments longer than the tile capacity: those longer than the
+// radix threshold for the LSD radix passes, the others for the merge passes.
+// Two forms write the same map and lists: one thread per segment boundary
 // (problems of long segments on average), or one warp-cooperative search per
 // half-tile (short segments, and batches).
 #pragma once
@@ -19,11 +20,14 @@ namespace segsort {
 constexpr int kBarrierSpinLimit = 1 << 24;  // ~2 s with the back-off below
 
 enum : int {
-  kCtrJobs = 0,      // long segments found by classify
-  kCtrItems = 2,     // merge items of all jobs
-  kCtrPasses = 3,    // most merge passes of any job
-  kCtrBarCount = 6,  // grid barrier: arrivals
-  kCtrBarGen = 7,    // grid barrier: generation
+  kCtrJobs = 0,       // segments for the merge passes found by classify
+  kCtrItems = 2,      // merge items of all jobs
+  kCtrPasses = 3,     // most merge passes of any job
+  kCtrBarCount = 6,   // grid barrier: arrivals
+  kCtrBarGen = 7,     // grid barrier: generation
+  kCtrRJobs = 8,      // segments for the radix passes found by classify
+  kCtrRTiles = 9,     // radix tiles of all radix jobs
+  kCtrRDigits = 10,   // OR over radix jobs of their digits that vary
   kCtrWords = 16,
 };
 
@@ -31,7 +35,7 @@ enum : int {
 template <typename K>
 struct LargeWs {
   uint32_t *ctr;          // [kCtrWords]
-  int4 *jobs;             // [max_jobs] long segments: {begin, end, 0, instance}
+  int4 *jobs;             // [max_jobs] merge segments: {begin, end, 0, instance}
   int32_t *item_prefix;   // [max_jobs + 1] merge items before each job
   int32_t *half_first;    // [halves + 1] first segment starting at or after h * CAP/2
   int32_t *item_job;      // [max_items] job of each merge item
@@ -39,9 +43,18 @@ struct LargeWs {
   int4 *item_desc;        // [2 * max_items] item descriptors of the current pass
   K *tmp_keys;            // [n]
   uint32_t *tmp_vals;     // [n]
+  int4 *rjobs;            // [max_rjobs] radix segments: {begin, end, 0, instance}
+  int32_t *rtile_prefix;  // [max_rjobs + 1] radix tiles before each radix job
+  int4 *rtile_desc;       // [max_rtiles] radix tiles: {first position, length, job, index in job}
+  uint32_t *rdigits;      // [max_rjobs] digits of the job's keys that vary (bit d: digit d)
+  uint32_t *rhist;        // [max_rjobs][digits][256] digit counts, then bucket starts
+  unsigned long long *rlook;  // [max_rtiles][256] look-back words of the radix tiles
   int32_t max_jobs;
+  int32_t max_rjobs;
   int64_t max_items;
   int64_t halves;
+  int64_t max_rtiles;
+  int64_t radix_min;      // segments longer than this take the radix passes
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -59,8 +72,9 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
 //  * half_first[h] = s for every half-tile h with off(s-1) < h*half <= off(s)
 //    (off(-1) = -inf, off(nseg) = +inf): the first segment starting in or
 //    after half-tile h, so the tile sort needs no search over the offsets;
-//  * segments longer than cap become jobs of the merge passes (warp-aggregated
-//    atomic append), tagged with the instance they belong to.
+//  * segments longer than cap become jobs of the merge passes, or of the
+//    radix passes when longer than ws.radix_min (warp-aggregated atomic
+//    appends), tagged with the instance they belong to.
 // Every lane of the warp calls it; `valid` is false for lanes past the end.
 template <typename K>
 __device__ __forceinline__ void classify_boundary(const Offsets &off, int64_t s, bool valid,
@@ -76,15 +90,36 @@ __device__ __forceinline__ void classify_boundary(const Offsets &off, int64_t s,
     for (int64_t h = h_lo; h <= h_hi; ++h) half_first[h] = static_cast<int32_t>(s);
     if (s < off.nseg) len = off(s + 1) - cur;
   }
-  const bool large = len > cap;
+  const bool rlarge = len > ws.radix_min;
+  const bool large = len > cap && !rlarge;
+  const int4 job = make_int4(static_cast<int32_t>(cur), static_cast<int32_t>(cur + len), 0, inst);
   const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, large);
-  if (ballot == 0) return;
-  uint32_t base = 0;
-  if (lane == 0) base = atomicAdd(&ws.ctr[kCtrJobs], __popc(ballot));
-  base = __shfl_sync(0xFFFFFFFFu, base, 0);
-  const uint32_t j = base + __popc(ballot & lanemask_lt());
-  if (large && j < static_cast<uint32_t>(ws.max_jobs))
-    ws.jobs[j] = make_int4(static_cast<int32_t>(cur), static_cast<int32_t>(cur + len), 0, inst);
+  if (ballot != 0) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&ws.ctr[kCtrJobs], __popc(ballot));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    const uint32_t j = base + __popc(ballot & lanemask_lt());
+    if (large && j < static_cast<uint32_t>(ws.max_jobs)) ws.jobs[j] = job;
+  }
+  const uint32_t rballot = __ballot_sync(0xFFFFFFFFu, rlarge);
+  if (rballot != 0) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&ws.ctr[kCtrRJobs], __popc(rballot));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    const uint32_t j = base + __popc(rballot & lanemask_lt());
+    if (rlarge && j < static_cast<uint32_t>(ws.max_rjobs)) ws.rjobs[j] = job;
+  }
+}
+
+// Appends one long segment to the merge or the radix job list.
+template <typename K>
+__device__ __forceinline__ void add_long_job(const LargeWs<K> &ws, int64_t beg, int64_t end,
+                                             int32_t inst) {
+  const int4 job = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end), 0, inst);
+  const bool radix = end - beg > ws.radix_min;
+  const uint32_t j = atomicAdd(&ws.ctr[radix ? kCtrRJobs : kCtrJobs], 1u);
+  if (j < static_cast<uint32_t>(radix ? ws.max_rjobs : ws.max_jobs))
+    (radix ? ws.rjobs : ws.jobs)[j] = job;
 }
 
 template <typename K>
@@ -153,11 +188,7 @@ large_classify_halves_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> 
     const int64_t a = lb_s[w], b = lb_s[w + 1];
     if (b > a) {
       const int64_t beg = off(b - 1), end = off(b);
-      if (end - beg > cap) {
-        const uint32_t j = atomicAdd(&ws.ctr[kCtrJobs], 1u);
-        if (j < static_cast<uint32_t>(ws.max_jobs))
-          ws.jobs[j] = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end), 0, 0);
-      }
+      if (end - beg > cap) add_long_job(ws, beg, end, 0);
     }
   }
 }
@@ -192,11 +223,7 @@ large_classify_halves_batch_kernel(const BatchInst *__restrict__ tab, int32_t co
     if (b > a) {
       const Offsets off = tab[i].offsets_view();
       const int64_t beg = off(b - 1), end = off(b);
-      if (end - beg > cap) {
-        const uint32_t j = atomicAdd(&ws.ctr[kCtrJobs], 1u);
-        if (j < static_cast<uint32_t>(ws.max_jobs))
-          ws.jobs[j] = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end), 0, i);
-      }
+      if (end - beg > cap) add_long_job(ws, beg, end, i);
     }
   }
 }
@@ -240,10 +267,9 @@ struct BatchSpace {
 
 // ---------------------------------------------------------------------------
 // Grid barrier for a cooperative launch (all CTAs resident), bounded: a CTA
-// that waits longer than kBarrierSpinLimit back-offs raises kStatusTimeout
-// and goes on, so a lost arrival can corrupt the result but never hang the
-// GPU.
-__device__ __forceinline__ void grid_barrier(uint32_t *ctr) {
+// that waits longer than spin_limit back-offs raises kStatusTimeout and goes
+// on, so a lost arrival can corrupt the result but never hang the GPU.
+__device__ __forceinline__ void grid_barrier(uint32_t *ctr, int spin_limit = kBarrierSpinLimit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const uint32_t gen = ld_volatile(ctr + kCtrBarGen);
@@ -256,7 +282,7 @@ __device__ __forceinline__ void grid_barrier(uint32_t *ctr) {
     } else {
       int spins = 0;
       while (ld_volatile(ctr + kCtrBarGen) == gen) {
-        if (++spins > kBarrierSpinLimit) {
+        if (++spins > spin_limit) {
           raise_status(kStatusTimeout);
           break;
         }

@@ -1,4 +1,6 @@
-// Long segments by merging: segments longer than the tile capacity CAP.
+// Long segments by merging: segments longer than the tile capacity CAP and
+// at most the radix threshold (longer ones take the radix passes of
+// radix_sort.cuh, which run first in the same cooperative kernel).
 //
 // The tile kernel has already sorted every CAP-chunk of each long segment
 // (its "runs", tile_cta), so a long segment of len elements is
@@ -31,6 +33,7 @@
 #include "segsort_common.cuh"
 #include "tile_sort.cuh"
 #include "classify.cuh"
+#include "radix_sort.cuh"
 
 namespace segsort {
 
@@ -177,9 +180,21 @@ __device__ __forceinline__ void load_ranges(const T *const (&src)[R], const int 
 template <typename K>
 constexpr int kMergeMinBlocks = sizeof(K) == 8 ? 2 : SEGSORT_MERGE_MINB;
 
+// Dynamic shared memory of the long-segment kernel: the larger of the radix
+// phases' and the merge passes' layouts.
+template <typename K, bool PAIRS>
+struct LongSmem {
+  static constexpr size_t kMerge = MergeSmem<K, PAIRS>::kBytes;
+  static constexpr size_t kRadix = RadixShape<K, PAIRS, kMThreads>::kBytes;
+  static constexpr size_t kBytes = kMerge > kRadix ? kMerge : kRadix;
+};
+
+// The long-segment kernel: the radix phases for the segments longer than
+// ws.radix_min, then the merge passes for the other segments longer than
+// cap.  Cooperative launch (every CTA resident).
 template <typename K, bool PAIRS, typename Space>
 __global__ void __launch_bounds__(kMThreads, kMergeMinBlocks<K>)
-merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
+long_segment_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
   using Ord = KeyOrder<K>;
   using MS = MergeSmem<K, PAIRS>;
   constexpr int NT = kMThreads;
@@ -191,11 +206,13 @@ merge_sort_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
   __shared__ uint64_t carry_s;
   __shared__ int maxp_s;
 
+  radix_phases<K, PAIRS, NT>(sp, ws, smem, warp_s);
+
   const int tid = threadIdx.x;
   const int64_t G = gridDim.x;
   const int64_t nj = min(static_cast<int64_t>(ld_volatile(&ws.ctr[kCtrJobs])),
                          static_cast<int64_t>(ws.max_jobs));
-  if (nj == 0) return;  // no long segments: one short launch
+  if (nj == 0) return;  // no segments for the merge passes
   const int4 *jobs = ws.jobs;
   int32_t *item_prefix = ws.item_prefix;   // [nj + 1] items before each job
   int32_t *item_job = ws.item_job;         // [items] job of each item

@@ -40,12 +40,10 @@ cudaEvent_t prof_event(cudaStream_t stream) {
 
 // Problems whose average segment is at most this long take the half-tile
 // classify and the streamed tile kernel (measured on GB300 over 2^24 pairs:
-// both faster up to 32, slower from 64).  Build-time knob; a huge value sends
-// every multi-tile problem through them.
-#ifndef SEGSORT_STREAM_MAX_AVG
-#define SEGSORT_STREAM_MAX_AVG 32
-#endif
-constexpr int64_t kStreamMaxAvgLen = SEGSORT_STREAM_MAX_AVG;
+// both faster up to 32, slower from 64).  Run-time parameter
+// (segsort_set_param); a huge value sends every multi-tile problem through
+// them.
+std::atomic<int64_t> g_stream_max_avg{32};
 
 // ---------------------------------------------------------------------------
 template <typename K, bool PAIRS>
@@ -77,7 +75,8 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // ---- one tile: every segment fits, no workspace, one kernel ---------------
   if (tiles == 1) {
     if (prof) rec.t0 = prof_event(stream);
-    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr, nullptr, nullptr);
+    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr, nullptr, nullptr,
+                                                          0);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     if (prof) {
       rec.t1 = prof_event(stream);
@@ -88,7 +87,9 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   }
 
   // ---- workspace ----------------------------------------------------------------
-  const WsLayout L = layout_for<K, PAIRS>(n);
+  // A caller's workspace is sized for every radix threshold
+  // (segsort_workspace_bytes); the library's own is sized for the current one.
+  const WsLayout L = ws != nullptr ? layout_any_threshold<K, PAIRS>(n) : layout_for<K, PAIRS>(n);
   bool owned = false;
   unsigned char *base = static_cast<unsigned char *>(ws);
   if (base == nullptr) {
@@ -105,6 +106,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   }
 
   LargeWs<K> W = ws_views<K, PAIRS>(base, L);
+  W.radix_min = std::max<int64_t>(L.radix_min, radix_min_for<K>());
 
   int rc = SEGSORT_OK;
   do {
@@ -116,7 +118,8 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // Short segments on average: one search per half-tile (work ~ n / CAP);
     // otherwise one thread per segment boundary (work ~ nseg, fewer rounds
     // of dependent loads).  The two write the same map and jobs.
-    const bool short_avg = n <= kStreamMaxAvgLen * static_cast<int64_t>(nseg);
+    const bool short_avg =
+        n <= g_stream_max_avg.load(std::memory_order_relaxed) * static_cast<int64_t>(nseg);
     if (short_avg) {
       const unsigned blocks =
           static_cast<unsigned>((W.halves + kClassifyWarps) / kClassifyWarps);  // halves + 1 entries
@@ -148,10 +151,11 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       const unsigned grid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(so) * S->sms, tiles));
       stream_kernel<<<grid, Cfg::NT, SL::kBytes, stream>>>(keys, vals, off, W.half_first,
-                                                           W.tmp_keys, W.tmp_vals, tiles);
+                                                           W.tmp_keys, W.tmp_vals, tiles,
+                                                           W.radix_min);
     } else {
       tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
-          keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals);
+          keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
     }
     if (prof) rec.t1 = prof_event(stream);
     if (cudaGetLastError() != cudaSuccess) {
@@ -159,10 +163,10 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       break;
     }
 
-    // ---- long segments: merge passes in one cooperative kernel (returns at
-    // once without long segments) ----------------------------------------------------
-    using MS = MergeSmem<K, PAIRS>;
-    auto merge_kernel = merge_sort_kernel<K, PAIRS, SingleSpace<K>>;
+    // ---- long segments: radix passes, then merge passes, in one cooperative
+    // kernel (returns at once without long segments) ----------------------------------
+    using MS = LongSmem<K, PAIRS>;
+    auto merge_kernel = long_segment_kernel<K, PAIRS, SingleSpace<K>>;
     static std::atomic<uint64_t> merge_attr_done{0};
     static std::atomic<int> merge_occ[kMaxDevices];
     if (!S->coop || ensure_smem(merge_kernel, MS::kBytes, merge_attr_done, dev) != cudaSuccess) {
@@ -200,7 +204,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
 
 template <typename K, bool PAIRS>
 size_t workspace_bytes_for(int64_t n) {
-  return layout_for<K, PAIRS>(n).total;
+  return layout_any_threshold<K, PAIRS>(n).total;
 }
 
 // ---------------------------------------------------------------------------
@@ -212,6 +216,9 @@ constexpr int64_t kNoAllocMaxN = SEGSORT_NOALLOC_MAX_N;
 constexpr size_t kNoAllocBytes =
     make_layout(kNoAllocMaxN, 4, 4, tile_cap<uint32_t>(), MergeShape<uint32_t>::T).total;
 static_assert(kNoAllocBytes > 0, "the no-allocation scratch must cover the long-segment path");
+// The documented figure: about 10 MiB on every GPU that loads the library.
+static_assert(kNoAllocBytes > (size_t{19} << 19) && kNoAllocBytes <= (size_t{21} << 19),
+              "the header, design and integration notes state about 10 MiB");
 
 struct NoAllocScratch {
   std::once_flag once;
@@ -231,6 +238,38 @@ void *noalloc_scratch(int dev) {
   NoAllocScratch &S = g_noalloc[dev];
   std::call_once(S.once, [&] { S.err = cudaGetSymbolAddress(&S.ptr, g_noalloc_scratch); });
   return S.err == cudaSuccess ? S.ptr : nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Self-test kernels of the bounded waits: each wait below can never complete,
+// and gives up after kSelftestSpins back-offs (a few milliseconds).
+constexpr int kSelftestSpins = 1 << 12;
+__device__ uint32_t g_selftest_ctr[kCtrWords];
+__device__ unsigned long long g_selftest_look[2 * kRBuckets];
+
+// A grid barrier CTA 1 never reaches (cooperative launch of two CTAs).
+__global__ void selftest_barrier_kernel() {
+  if (blockIdx.x != 0) return;
+  grid_barrier(g_selftest_ctr, kSelftestSpins);
+}
+
+// An mbarrier phase expecting 16 bytes that no copy supplies.
+__global__ void selftest_mbar_kernel() {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(&bar, 16);
+    if (!mbar_wait(&bar, 0, kSelftestSpins)) raise_status(kStatusTimeout);
+  }
+}
+
+// The look-back of tile 1 of a segment whose tile 0 never publishes.
+__global__ void selftest_look_kernel() {
+  look_back(g_selftest_look, 1, 1, static_cast<int>(threadIdx.x), 1u, 0, kSelftestSpins);
 }
 }  // namespace
 }  // namespace segsort
@@ -328,6 +367,94 @@ int segsort_device_status(int clear) {
   }
   if (segsort::batch_device_status(clear != 0, &vb) != cudaSuccess) return SEGSORT_ERR_CUDA;
   return ((v | vb) & segsort::kStatusTimeout) ? SEGSORT_ERR_TIMEOUT : SEGSORT_OK;
+}
+
+int segsort_pool_bytes(int *created, uint64_t *used) {
+  using namespace segsort;
+  if (created == nullptr || used == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  DeviceState *S = device_state(dev);
+  if (S == nullptr) return SEGSORT_ERR_CUDA;
+  *created = 0;
+  *used = 0;
+  if (!S->pool_made.load(std::memory_order_acquire)) return SEGSORT_OK;
+  *created = 1;
+  uint64_t v = 0;
+  if (cudaMemPoolGetAttribute(S->pool, cudaMemPoolAttrUsedMemCurrent, &v) != cudaSuccess)
+    return SEGSORT_ERR_CUDA;
+  *used = v;
+  return SEGSORT_OK;
+}
+
+int segsort_set_param(int param, int64_t value) {
+  using namespace segsort;
+  switch (param) {
+    case SEGSORT_PARAM_RADIX_MIN_32:
+      if (value < kRadixMinFloor) return SEGSORT_ERR_INVALID_ARG;
+      g_radix_min32.store(value, std::memory_order_relaxed);
+      return SEGSORT_OK;
+    case SEGSORT_PARAM_RADIX_MIN_64:
+      if (value < kRadixMinFloor) return SEGSORT_ERR_INVALID_ARG;
+      g_radix_min64.store(value, std::memory_order_relaxed);
+      return SEGSORT_OK;
+    case SEGSORT_PARAM_STREAM_MAX_AVG:
+      if (value < 0) return SEGSORT_ERR_INVALID_ARG;
+      g_stream_max_avg.store(value, std::memory_order_relaxed);
+      return SEGSORT_OK;
+    default:
+      return SEGSORT_ERR_INVALID_ARG;
+  }
+}
+
+int segsort_get_param(int param, int64_t *value) {
+  using namespace segsort;
+  if (value == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  switch (param) {
+    case SEGSORT_PARAM_RADIX_MIN_32: *value = radix_min_for<uint32_t>(); return SEGSORT_OK;
+    case SEGSORT_PARAM_RADIX_MIN_64: *value = radix_min_for<uint64_t>(); return SEGSORT_OK;
+    case SEGSORT_PARAM_STREAM_MAX_AVG:
+      *value = g_stream_max_avg.load(std::memory_order_relaxed);
+      return SEGSORT_OK;
+    default:
+      return SEGSORT_ERR_INVALID_ARG;
+  }
+}
+
+int segsort_selftest_wait_timeout(int which) {
+  using namespace segsort;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  cudaError_t e = cudaSuccess;
+  switch (which) {
+    case 0: {
+      const uint32_t zero[kCtrWords] = {};
+      e = cudaMemcpyToSymbolAsync(g_selftest_ctr, zero, sizeof(zero), 0, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(selftest_barrier_kernel),
+                                        dim3(2), dim3(32), nullptr, 0, st);
+      break;
+    }
+    case 1:
+      selftest_mbar_kernel<<<1, 32, 0, st>>>();
+      e = cudaGetLastError();
+      break;
+    case 2: {
+      static const unsigned long long zero[2 * kRBuckets] = {};
+      e = cudaMemcpyToSymbolAsync(g_selftest_look, zero, sizeof(zero), 0, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) {
+        selftest_look_kernel<<<1, kRBuckets, 0, st>>>();
+        e = cudaGetLastError();
+      }
+      break;
+    }
+    default:
+      cudaStreamDestroy(st);
+      return SEGSORT_ERR_INVALID_ARG;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return e == cudaSuccess ? SEGSORT_OK : SEGSORT_ERR_CUDA;
 }
 
 const char *segsort_error_string(int code) {

@@ -2,8 +2,8 @@
 //
 // The instances of a batch are grouped by key type.  A group is sorted by the
 // same three kernels as one plain call -- classify, the tile sort, the
-// cooperative merge passes for long segments -- launched once for the whole
-// group: every kernel finds an instance through a device table (BatchInst),
+// cooperative long-segment kernel (radix passes, then merge passes) --
+// launched once for the whole group: every kernel finds an instance through a device table (BatchInst),
 // tile-sort CTAs and classify warps by binary search over the instances'
 // bases, and long-segment jobs through the instance index they carry.  Small instances
 // therefore share CTAs' worth of work with large ones instead of paying a
@@ -60,6 +60,10 @@ int64_t item_of(int type) {
   return type == SEGSORT_KEY_U64 ? MergeShape<uint64_t>::T : MergeShape<uint32_t>::T;
 }
 
+int64_t radix_min_of(int type) {
+  return type == SEGSORT_KEY_U64 ? radix_min_for<uint64_t>() : radix_min_for<uint32_t>();
+}
+
 // Validates the items and lays out every group.  Empty items (n == 0 or
 // nseg == 0) have nothing to sort and are left out.
 int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B) {
@@ -97,7 +101,8 @@ int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B)
   for (int t = 0; t < kKeyTypes; ++t) {
     Group &G = g[t];
     if (G.insts.empty()) continue;
-    G.L = make_layout(G.total_n, key_bytes_of(t), 4, cap_of(t), item_of(t), G.half_entries);
+    G.L = make_layout(G.total_n, key_bytes_of(t), 4, cap_of(t), item_of(t), G.half_entries,
+                      radix_min_of(t));
     G.tab_off = off;
     off = align256(off + G.insts.size() * sizeof(BatchInst));
     G.ws_off = off;
@@ -141,10 +146,10 @@ cudaError_t upload_table(const std::vector<BatchInst> &v, BatchInst *dst, cudaSt
 template <typename K>
 struct BatchKernels {
   using TCfg = typename TileFor<K, true>::Cfg;
-  using MS = MergeSmem<K, true>;
+  using MS = LongSmem<K, true>;
   static constexpr auto tile = tile_sort_batch_kernel<K, true, TCfg::NT, TCfg::KPT,
                                                       TileFor<K, true>::kMinBlocks>;
-  static constexpr auto merge = merge_sort_kernel<K, true, BatchSpace<K>>;
+  static constexpr auto merge = long_segment_kernel<K, true, BatchSpace<K>>;
   static constexpr auto classify = large_classify_halves_batch_kernel<K>;
   static inline std::atomic<uint64_t> tile_attr{0}, merge_attr{0};
   static inline std::atomic<int> merge_occ[kMaxDevices];
@@ -171,9 +176,10 @@ struct BatchKernels {
                                                                    cap / 2, W);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
 
-    // Tile sort first: it forms the sorted runs the merge passes read.
+    // Tile sort first: it forms the sorted runs the merge passes read (the
+    // radix passes read the caller's buffers, which it leaves alone).
     tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, TCfg::kSmemBytes, stream>>>(
-        tab, count, W.half_first, W.tmp_keys, W.tmp_vals);
+        tab, count, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     const int64_t items = G.total_n / MergeShape<K>::T + 1;

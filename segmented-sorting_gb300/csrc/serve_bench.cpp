@@ -5,8 +5,11 @@
 //
 //   serve_bench.exe [--requests R] [--rates 1000,5000,10000,50000]
 //                   [--budget-gb 64] [--seed 7] [--lo-log 10] [--hi-log 24]
-//                   [--verify-every 40] [--depth 2] [--max-batch 0]
+//                   [--verify-every V] [--depth 2] [--max-batch 0]
 //                   [--max-batch-keys 0]
+//
+// V defaults to max(40, R / 200): about 200 verified requests whatever R is
+// (each holds four pinned result buffers of its own).
 //
 // Request r: n log-uniform in [2^lo, 2^hi]; segment lengths lognormal(4, 2.5)
 // clipped to [1, 2^22], summed to n, 1% empty segments inserted; keys and
@@ -86,7 +89,7 @@ struct Req {
   int64_t n;
   int64_t start;  // slice of the pool
   std::vector<int32_t> off;
-  int32_t *h_off;  // pinned copy
+  int32_t *h_off;  // its place in the pinned arena of every request's offsets
   double arrival_unit;  // arrival time at rate 1 req/s (seconds)
   bool verify;
 };
@@ -113,7 +116,7 @@ int main(int argc, char **argv) {
   double budget_gb = 64.0;
   uint64_t seed = 7;
   double lo_log = 10, hi_log = 24;
-  int verify_every = 40, depth = 2, max_batch = 0, pool_log = 25;
+  int verify_every = 0, depth = 2, max_batch = 0, pool_log = 25;
   int64_t max_batch_keys = 0;
   for (int i = 1; i + 1 < argc; i += 2) {
     const std::string a = argv[i], v = argv[i + 1];
@@ -138,6 +141,7 @@ int main(int argc, char **argv) {
       }
     }
   }
+  if (verify_every <= 0) verify_every = static_cast<int>(std::max<int64_t>(40, requests / 200));
   check(cudaSetDevice(0), "cudaSetDevice");
 
   // ---- requests ------------------------------------------------------------
@@ -156,13 +160,22 @@ int main(int argc, char **argv) {
     q.n = std::min<int64_t>(pool_n, static_cast<int64_t>(std::llround(std::exp2(lo_log + (hi_log - lo_log) * u))));
     q.start = static_cast<int64_t>(draw(seed, 8, 3 * r + 1) % static_cast<uint64_t>(pool_n - q.n + 1));
     q.off = lognormal_offsets(q.n, seed * 100003 + r);
-    q.h_off = pinned<int32_t>(q.off.size());
-    std::memcpy(q.h_off, q.off.data(), q.off.size() * 4);
     t += -std::log(unit(draw(seed, 9, r)));
     q.arrival_unit = t;
     q.verify = verify_every > 0 && r % verify_every == 0;
     total_keys += q.n;
     max_n = std::max(max_n, q.n);
+  }
+  // Every request's offsets in one pinned arena (one allocation, however
+  // many requests).
+  size_t arena_n = 0;
+  for (const Req &q : reqs) arena_n += q.off.size();
+  int32_t *arena = pinned<int32_t>(arena_n);
+  size_t at = 0;
+  for (Req &q : reqs) {
+    q.h_off = arena + at;
+    std::memcpy(q.h_off, q.off.data(), q.off.size() * 4);
+    at += q.off.size();
   }
   uint32_t *sink_k = pinned<uint32_t>(max_n), *sink_v = pinned<uint32_t>(max_n);
   std::vector<uint32_t *> out_srv_k(requests, nullptr), out_srv_v(requests, nullptr);

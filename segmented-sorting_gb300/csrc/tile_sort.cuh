@@ -104,17 +104,6 @@ template <> struct WordTraits<uint64_t> {
   }
 };
 
-// Chunks whose sort needs more merge levels than this take the radix path,
-// when it is compiled in (SEGSORT_TILE_RADIX=1).  Off by default: measured on
-// GB300 its random-rank scatter makes it shared-memory bound and slower than
-// the merge levels it replaces.
-#ifndef SEGSORT_TILE_RADIX
-#define SEGSORT_TILE_RADIX 0
-#endif
-#ifndef SEGSORT_MERGE_LEVELS_MAX
-#define SEGSORT_MERGE_LEVELS_MAX 2
-#endif
-
 // ---------------------------------------------------------------------------
 // Shared-memory layout and launch shape of one tile-sort instantiation.
 // ---------------------------------------------------------------------------
@@ -143,10 +132,7 @@ struct TileConfig {
   static constexpr size_t kMainBytes =
       ((kWordBytes > kOutBytes ? kWordBytes : kOutBytes) + 15) / 16 * 16;
   static constexpr size_t kValBytes = PAIRS ? CAP * sizeof(uint32_t) : 0;
-  // Radix path (32-bit keys): per-thread digit counters, 16 digits x NT.
-  static constexpr bool kRadix = sizeof(Bits) == 4;
-  static constexpr size_t kCntBytes = (kRadix && SEGSORT_TILE_RADIX) ? 16 * NT * sizeof(uint32_t) : 0;
-  static constexpr size_t kSmemBytes = kMainBytes + kValBytes + kCntBytes;
+  static constexpr size_t kSmemBytes = kMainBytes + kValBytes;
 
   static __device__ __forceinline__ int wslot(int i) { return i + i / WUNIT; }
   static __device__ __forceinline__ int oslot(int i) { return i + (i >> 5); }
@@ -423,102 +409,6 @@ __device__ __forceinline__ uint32_t block_exclusive_add(uint32_t v, uint32_t &to
   return before + x - v;
 }
 
-// Block-wide OR and AND of one value per thread.
-template <int NT>
-__device__ __forceinline__ void block_or_and(uint32_t v_or, uint32_t v_and, uint32_t &r_or,
-                                             uint32_t &r_and, int *warp_s) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t o = __reduce_or_sync(0xFFFFFFFFu, v_or);
-  const uint32_t a = __reduce_and_sync(0xFFFFFFFFu, v_and);
-  __shared__ uint32_t and_s[NT / 32];
-  if (lane == 0) {
-    warp_s[warp] = static_cast<int>(o);
-    and_s[warp] = a;
-  }
-  __syncthreads();
-  r_or = 0u;
-  r_and = 0xFFFFFFFFu;
-#pragma unroll
-  for (int w = 0; w < NT / 32; ++w) {
-    r_or |= static_cast<uint32_t>(warp_s[w]);
-    r_and &= and_s[w];
-  }
-  __syncthreads();
-}
-
-// Block-wide maximum of one value per thread.
-template <int NT>
-__device__ __forceinline__ int block_max(int v, int *warp_s) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int x = static_cast<int>(__reduce_max_sync(0xFFFFFFFFu, static_cast<unsigned>(v + 1))) - 1;
-  if (lane == 0) warp_s[warp] = x;
-  __syncthreads();
-  int r = -1;
-#pragma unroll
-  for (int w = 0; w < NT / 32; ++w) r = max(r, warp_s[w]);
-  __syncthreads();
-  return r;
-}
-
-// One stable counting pass of the CTA-wide radix sort over the 4-bit digit at
-// bit `shift` of 64-bit words.  Thread t holds positions [t*KPT, t*KPT+KPT)
-// in w[]; afterwards it holds the same positions of the new order.  Counts
-// live in cnt[digit][thread]; their exclusive prefix in (digit, thread)
-// order is the first output slot of each (digit, thread) pair, so equal
-// digits keep their order (stability).
-template <typename Cfg>
-__device__ __forceinline__ void radix_pass(uint64_t (&w)[Cfg::KPT], int shift, uint64_t *W,
-                                           uint32_t *cnt, int *warp_s) {
-  constexpr int NT = Cfg::NT;
-  constexpr int KPT = Cfg::KPT;
-  const int tid = threadIdx.x;
-  uint4 *cnt4 = reinterpret_cast<uint4 *>(cnt);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) cnt4[i * NT + tid] = make_uint4(0, 0, 0, 0);
-  __syncthreads();
-  uint32_t loc[KPT];
-#pragma unroll
-  for (int j = 0; j < KPT; ++j) {
-    const uint32_t d = static_cast<uint32_t>(w[j] >> shift) & 15u;
-    uint32_t *c = cnt + d * NT + tid;
-    loc[j] = *c;
-    *c = loc[j] + 1;
-  }
-  __syncthreads();
-  // Exclusive prefix over cnt[0, 16 * NT) in index order; thread t scans
-  // entries [16t, 16t + 16).
-  uint32_t v[16];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const uint4 x = cnt4[tid * 4 + q];
-    v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
-  }
-  uint32_t run = 0;
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const uint32_t c = v[q];
-    v[q] = run;
-    run += c;
-  }
-  uint32_t total;
-  const uint32_t base = block_exclusive_add<NT>(run, total, warp_s);
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-    cnt4[tid * 4 + q] = make_uint4(v[4 * q] + base, v[4 * q + 1] + base, v[4 * q + 2] + base,
-                                   v[4 * q + 3] + base);
-  __syncthreads();
-#pragma unroll
-  for (int j = 0; j < KPT; ++j) {
-    const uint32_t d = static_cast<uint32_t>(w[j] >> shift) & 15u;
-    const int r = static_cast<int>(cnt[d * NT + tid] + loc[j]);
-    W[Cfg::wslot(r)] = w[j];
-  }
-  __syncthreads();
-  const int base_pos = tid * KPT;
-#pragma unroll
-  for (int j = 0; j < KPT; ++j) w[j] = W[Cfg::wslot(base_pos + j)];
-}
-
 // Writes a sorted chunk: thread t holds the words of positions
 // [t*KPT, t*KPT+KPT); they are staged as keys and gathered values in shared
 // memory (over the word buffer, which must no longer be read) and stored with
@@ -644,75 +534,6 @@ __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsign
   uint32_t *Vs = reinterpret_cast<uint32_t *>(smem + Cfg::kMainBytes);
   const int tid = threadIdx.x;
   const int base = tid * KPT;
-
-  // ---- path choice: merge levels this chunk needs ------------------------------
-  // The merge at level l joins runs of KPT * 2^l elements; it has work only
-  // where a run boundary (an odd multiple of KPT * 2^l) falls inside a
-  // segment.  Thread t's block boundary KPT * t is such a boundary for level
-  // ctz(t).
-  if constexpr (Cfg::kRadix && SEGSORT_TILE_RADIX) {
-    int need = -1;
-    if (tid > 0 && base < m) {
-      const bool head = multi ? ((hb[base >> 5] >> (base & 31)) & 1u) != 0 : false;
-      if (!head) need = __ffs(tid) - 1;
-    }
-    const int levels = block_max<NT>(need, warp_s) + 1;
-    if (levels > SEGSORT_MERGE_LEVELS_MAX) {
-      // ---- radix path: LSD on (segment id, key order bits), 4-bit digits ----
-      uint64_t *W64 = reinterpret_cast<uint64_t *>(smem);
-      uint32_t *cnt = reinterpret_cast<uint32_t *>(smem + Cfg::kMainBytes + Cfg::kValBytes);
-      constexpr uint32_t kLow = KPT >= 32 ? 0xFFFFFFFFu : ((1u << KPT) - 1);
-      const uint32_t mask = (multi && base < m) ? (hb[base >> 5] >> (base & 31)) & kLow : 0u;
-      uint32_t nsegs = 1;
-      const uint32_t seg_before =
-          multi ? block_exclusive_add<NT>(static_cast<uint32_t>(__popc(mask)), nsegs, warp_s) : 0u;
-      uint64_t w[KPT];
-      uint32_t k_or = 0u, k_and = 0xFFFFFFFFu;
-#pragma unroll
-      for (int j = 0; j < KPT; ++j) {
-        const int i = base + j;
-        if (i < m) {
-          const uint64_t x = static_cast<uint64_t>(W[Cfg::wslot(i)]);
-          const uint32_t bits = static_cast<uint32_t>(x >> 16);
-          const uint32_t sid =
-              multi ? seg_before + __popc(mask & ((2u << j) - 1u)) - 1u : 0u;
-          w[j] = (static_cast<uint64_t>(bits) << 32) | (sid << 12) | static_cast<uint32_t>(i);
-          k_or |= bits;
-          k_and &= bits;
-        } else {
-          w[j] = ~0ull;  // sorts last in every pass
-        }
-      }
-      uint32_t all_or, all_and;
-      block_or_and<NT>(k_or, k_and, all_or, all_and, warp_s);
-      const uint32_t varying = all_or ^ all_and;
-      __syncthreads();  // W is rewritten by the passes
-#pragma unroll 1
-      for (int q = 0; q < 8; ++q)
-        if ((varying >> (4 * q)) & 15u) radix_pass<Cfg>(w, 32 + 4 * q, W64, cnt, warp_s);
-      if (multi && nsegs > 1) {
-        const int seg_bits = 32 - __clz(nsegs - 1);
-#pragma unroll 1
-        for (int q = 0; q * 4 < seg_bits; ++q) radix_pass<Cfg>(w, 12 + 4 * q, W64, cnt, warp_s);
-      }
-      __syncthreads();
-#pragma unroll
-      for (int j = 0; j < KPT; ++j) {
-        const int i = base + j;
-        if (i < m) {
-          KO[Cfg::oslot(i)] = Ord::from_bits(static_cast<typename Cfg::Bits>(w[j] >> 32));
-          if constexpr (PAIRS) VO[Cfg::oslot(i)] = Vs[static_cast<uint32_t>(w[j]) & 0xFFFu];
-        }
-      }
-      __syncthreads();
-      const auto out = dst();
-      store_range<NT>(out.dst_keys, m, [&](int i) { return KO[Cfg::oslot(i)]; });
-      if constexpr (PAIRS)
-        store_range<NT>(out.dst_vals, m, [&](int i) { return VO[Cfg::oslot(i)]; });
-      __syncthreads();
-      return;
-    }
-  }
 
   // ---- blocked words + segment field ------------------------------------------
   // The merge at level l joins runs of KPT * 2^l words and has work only where
@@ -916,7 +737,8 @@ struct TilePlan {
 // every segment).  runs: the caller forms the CAP-runs of long segments.
 //
 // With runs, the plan also holds the sorted runs of long segments (longer
-// than CAP) for the merge passes: every CAP-chunk [b + k*CAP, ...) of such a
+// than CAP, at most radix_min: longer ones take the radix passes and are not
+// touched here) for the merge passes: every CAP-chunk [b + k*CAP, ...) of such a
 // segment is sorted by the CTA of the tile its first element lies in, into
 // the buffer the segment's first merge pass reads (the caller's buffers when
 // the segment needs an even number of passes, tmp otherwise, so that its last
@@ -925,7 +747,7 @@ struct TilePlan {
 // segment starting in each of its halves.  One thread computes a plan.
 template <int CAP>
 __device__ __forceinline__ void plan_tile(const Offsets &off, const int32_t *__restrict__ half_first,
-                                          int64_t t, bool runs, TilePlan &P) {
+                                          int64_t t, bool runs, int64_t radix_min, TilePlan &P) {
   constexpr int64_t HALF = CAP / 2;
   const int64_t nseg = off.nseg;
   int nc = 0;
@@ -942,7 +764,7 @@ __device__ __forceinline__ void plan_tile(const Offsets &off, const int32_t *__r
   auto add_run = [&](int64_t s, int64_t c) {
     if (!runs) return;
     const int64_t b = off(s), e = off(s + 1);
-    if (e - b <= CAP || c < b || c >= e) return;
+    if (e - b <= CAP || e - b > radix_min || c < b || c >= e) return;
     P.c[nc] = TileChunk{c, static_cast<int32_t>(s), static_cast<int32_t>(s),
                         static_cast<int32_t>(min(static_cast<int64_t>(CAP), e - c)),
                         merge_passes(e - b, CAP) & 1};
@@ -1023,13 +845,15 @@ __device__ __forceinline__ void sort_tile_chunk(const TileChunk &C, K *keys, uin
 // ---------------------------------------------------------------------------
 // One CTA of the tile sort: tile t of a problem whose half-tile map is
 // half_first (null: the problem is one tile).  With tmp_keys given the CTA
-// also forms the CAP-runs of long segments (plan_tile).
+// also forms the CAP-runs of the long segments of at most radix_min
+// elements (plan_tile).
 // ---------------------------------------------------------------------------
 template <typename K, bool PAIRS, int NT, int KPT>
 __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restrict__ vals,
                                          const Offsets &off, const int32_t *__restrict__ half_first,
                                          int64_t t, K *__restrict__ tmp_keys = nullptr,
-                                         uint32_t *__restrict__ tmp_vals = nullptr) {
+                                         uint32_t *__restrict__ tmp_vals = nullptr,
+                                         int64_t radix_min = 0) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ TilePlan plan_s;
@@ -1037,7 +861,8 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
   __shared__ int warp_s[NT / 16];
 
   if (t * Cfg::CAP >= off.n) return;
-  if (threadIdx.x == 0) plan_tile<Cfg::CAP>(off, half_first, t, tmp_keys != nullptr, plan_s);
+  if (threadIdx.x == 0)
+    plan_tile<Cfg::CAP>(off, half_first, t, tmp_keys != nullptr, radix_min, plan_s);
   __syncthreads();
   const int nc = plan_s.nc;
   for (int c = 0; c < nc; ++c)
@@ -1052,8 +877,9 @@ template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                  const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
-                 uint32_t *__restrict__ tmp_vals) {
-  tile_cta<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x, tmp_keys, tmp_vals);
+                 uint32_t *__restrict__ tmp_vals, int64_t radix_min) {
+  tile_cta<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x, tmp_keys, tmp_vals,
+                              radix_min);
 }
 
 // ---------------------------------------------------------------------------
@@ -1066,13 +892,13 @@ template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_sort_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
                        const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
-                       uint32_t *__restrict__ tmp_vals) {
+                       uint32_t *__restrict__ tmp_vals, int64_t radix_min) {
   const int64_t t = blockIdx.x;
   const int32_t i = find_instance(tab, count, t, &BatchInst::tile_base);
   const BatchInst &I = tab[i];
   tile_cta<K, PAIRS, NT, KPT>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
                               half_first + I.half_base, t - I.tile_base, tmp_keys + I.tmp_base,
-                              PAIRS ? tmp_vals + I.tmp_base : nullptr);
+                              PAIRS ? tmp_vals + I.tmp_base : nullptr, radix_min);
 }
 
 }  // namespace segsort

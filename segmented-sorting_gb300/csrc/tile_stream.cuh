@@ -21,7 +21,8 @@
 // Chunk plans (plan_tile) are computed 16 tiles at a time by lanes of warp 0
 // into a ring of 32, one batch ahead of the copies that need them.
 // Every wait on the mbarrier is bounded; a wait that gives up raises
-// kStatusTimeout and the CTA returns.
+// kStatusTimeout, waits once more (bounded) for the copies of that stage --
+// the only ones the CTA has in flight -- and the CTA returns.
 #pragma once
 
 #include "tile_sort.cuh"
@@ -75,8 +76,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 // Waits for the completion of the barrier phase with the given parity;
 // false when it did not complete within the spin limit.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (int it = 0; it < kStageSpinLimit; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          int spin_limit = kStageSpinLimit) {
+  for (int it = 0; it < spin_limit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it >= 8) __nanosleep(64);
   }
@@ -168,7 +170,7 @@ template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_stream_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                    const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
-                   uint32_t *__restrict__ tmp_vals, int64_t ntiles) {
+                   uint32_t *__restrict__ tmp_vals, int64_t ntiles, int64_t radix_min) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   using SL = StreamLayout<Cfg, K, PAIRS>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -191,7 +193,7 @@ tile_stream_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
     if (tid < 32) {
       const int64_t i = i0 + tid;
       if (tid < kPlanBatch && i < iters)
-        plan_tile<Cfg::CAP>(off, half_first, t0 + i * G, runs, plans[i % kPlanRing]);
+        plan_tile<Cfg::CAP>(off, half_first, t0 + i * G, runs, radix_min, plans[i % kPlanRing]);
       __syncwarp();
     }
   };
@@ -236,7 +238,16 @@ tile_stream_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
     if (nc > 0) clear_heads<NT>(hb, m, multi);
     const bool ok = mbar_wait(&bar, static_cast<uint32_t>(i & 1));
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) raise_status(kStatusTimeout);
+      // The copies of this stage are the only ones the CTA has issued and not
+      // seen complete (the next stage is issued only after this wait).  A
+      // timeout means their bytes have not all arrived; wait for them once
+      // more, bounded, so that the CTA does not end while a copy may still
+      // write its shared memory, then give up on the rest of the tiles.
+      if (tid == 0) {
+        raise_status(kStatusTimeout);
+        mbar_wait(&bar, static_cast<uint32_t>(i & 1));
+      }
+      __syncthreads();
       return;
     }
     // ---- staged chunk -> words, values, segment heads -----------------------

@@ -43,11 +43,32 @@ def test_python_binding_covers_the_header(pkg):
 
 
 def test_library_is_built_for_sm_103a(pkg):
-    out = subprocess.run(["cuobjdump", "--list-elf", str(pkg.LIB_PATH)],
-                         capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+    from importlib import util
+    spec = util.spec_from_file_location("_segsort_build_check", ROOT / "segmented-sorting_gb300" / "build.py")
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    assert mod.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    assert all("sm_103a" in " ".join(mod._obj_cmd(u)) for u in mod.LIB_UNITS)
+
+
+def test_run_time_parameters(pkg):
+    """segsort_set_param / segsort_get_param are host-side only."""
+    L = pkg.lib()
+    saved = {p: pkg.get_param(p) for p in (pkg.PARAM_RADIX_MIN_32, pkg.PARAM_RADIX_MIN_64,
+                                            pkg.PARAM_STREAM_MAX_AVG)}
+    assert saved[pkg.PARAM_RADIX_MIN_32] >= 4096 and saved[pkg.PARAM_RADIX_MIN_64] >= 4096
+    with pkg.params({pkg.PARAM_RADIX_MIN_32: 1 << 20, pkg.PARAM_STREAM_MAX_AVG: 0}):
+        assert pkg.get_param(pkg.PARAM_RADIX_MIN_32) == 1 << 20
+        assert pkg.get_param(pkg.PARAM_STREAM_MAX_AVG) == 0
+    assert {p: pkg.get_param(p) for p in saved} == saved
+    # below the floor, negative, unknown parameter, missing output
+    assert L.segsort_set_param(pkg.PARAM_RADIX_MIN_32, 4095) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_set_param(pkg.PARAM_RADIX_MIN_64, 100) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_set_param(pkg.PARAM_STREAM_MAX_AVG, -1) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_set_param(99, 1) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_get_param(99, ctypes.byref(ctypes.c_int64())) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_get_param(pkg.PARAM_RADIX_MIN_32, None) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert {p: pkg.get_param(p) for p in saved} == saved
 
 
 def test_host_side_argument_checks(pkg):
@@ -150,7 +171,8 @@ def test_server_host_side_argument_checks(pkg):
     items = (pkg.BatchItem * 2)(pkg.BatchItem(0, 0, 16, 16, 1 << 20, 16, 4, 0),
                                 pkg.BatchItem(3, 0, 16, 16, 5000, 16, 2, 0))
     ws = L.segsort_batch_workspace_bytes(items, 2)
-    assert ws > L.segsort_workspace_bytes(1 << 20, 4, 4, 4)
+    # at least the ping-pong copies of both items' keys and values
+    assert ws > 8 * (1 << 20) + 12 * 5000
     assert L.segsort_batch_workspace_bytes(items, -1) == 0
 
 

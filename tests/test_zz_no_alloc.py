@@ -47,6 +47,52 @@ def test_no_alloc_matches_allocating_entry_point_on_two_calls(pkg, cuda, inst):
         assert np.array_equal(v, v_ref)
 
 
+_FRESH_PROCESS = r"""
+import ctypes, sys
+import numpy as np
+import torch
+sys.path.insert(0, {root!r})
+import __graft_entry__ as entry
+pkg = entry.load_package()
+inst = __import__(entry.PKG_NAME + ".instances", fromlist=["x"])
+L = pkg.lib()
+made, used = ctypes.c_int(), ctypes.c_uint64()
+def pool():
+    assert L.segsort_pool_bytes(ctypes.byref(made), ctypes.byref(used)) == 0
+    return made.value, used.value
+n = 300000
+off = torch.from_numpy(inst.diff_offsets(n, 9, seed=91)).cuda()
+k = torch.from_numpy(inst.uniform_keys(n, seed=91).view(np.int32)).cuda()
+v = torch.arange(n, dtype=torch.int32, device="cuda")
+st = torch.cuda.current_stream().cuda_stream
+assert pool() == (0, 0)
+for _ in range(2):
+    assert L.segsort_pairs_u32_noalloc(k.data_ptr(), v.data_ptr(), n, off.data_ptr(), 9, st) == 0
+    torch.cuda.synchronize()
+    assert pool() == (0, 0), pool()
+# the allocating entry point creates the pool on its first long-segment call
+assert L.segsort_pairs_u32(k.data_ptr(), v.data_ptr(), n, off.data_ptr(), 9, st) == 0
+torch.cuda.synchronize()
+assert pool()[0] == 1, pool()
+print("pool untouched by the allocation-free calls")
+"""
+
+
+@pytest.mark.gpu
+def test_no_alloc_never_creates_the_library_pool(pkg, cuda):
+    """In a fresh process, calls of the allocation-free entry point leave the
+    library's own memory pool uncreated; the allocating entry point then
+    creates it.  A regression that let the no-allocation path fall back to
+    the pool would fail here even though its results stay exact."""
+    import subprocess
+    import sys
+    from conftest import ROOT
+    r = subprocess.run([sys.executable, "-c", _FRESH_PROCESS.format(root=str(ROOT))],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "pool untouched" in r.stdout
+
+
 @pytest.mark.gpu
 def test_no_alloc_rejects_sizes_beyond_its_scratch(pkg, cuda):
     L = pkg.lib()
