@@ -20,7 +20,10 @@
 //   pass d   per tile (CTA b takes tiles b, b + G, ...; every CTA of the
 //            cooperative grid is resident and a tile waits only on the tiles
 //            before it, so the CTA holding the lowest unfinished tile always
-//            makes progress): the tile's keys and values arrive in a staging
+//            makes progress; when every segment has the same number of tiles,
+//            tile t is tile t / nj of segment t mod nj, so that the tiles in
+//            flight at once spread over the segments and their look-back
+//            chains stay short): the tile's keys and values arrive in a staging
 //            buffer by bulk asynchronous copy, issued while the CTA was
 //            finishing the tile before; the stable rank of every key among
 //            the tile's keys of its digit (lanes with equal digits found by
@@ -97,11 +100,13 @@ struct RadixShape {
 
 // A tile as thread 0 describes it to the CTA: its index, segment (job),
 // first position and length within the instance, index within the
-// segment, the buffer it is read from, whether its segment varies in the
-// pass's digit.
+// segment, the tile number of its look-back words (segment-major, so that a
+// tile's predecessors are the numbers just below), the buffer it is read
+// from, whether its segment varies in the pass's digit.
 struct RadixSlot {
   int64_t t;
-  int32_t j, a, cnt, k, from_tmp, active;
+  int32_t j, a, cnt, k, w, from_tmp, active;
+  int32_t pad;
 };
 
 // Radix tiles of a segment of len keys.
@@ -262,6 +267,7 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
   const bool local = nj <= RS::kLocalJobs;
   int32_t *lpre = reinterpret_cast<int32_t *>(smem + RS::kStageK);  // [nj + 1] when local
   int64_t ntiles;
+  bool interleave;
   {
     const int per = (nj + NT - 1) / NT;
     const int j0 = min(tid * per, nj), j1 = min(j0 + per, nj);
@@ -271,6 +277,30 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       const int4 jb = ws.rjobs[j];
       sum += static_cast<uint32_t>(radix_tiles<TILE>(jb.y > jb.x ? jb.y - jb.x : 0));
     }
+    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+    for (int j = j0; j < j1; ++j) {
+      const int4 jb = ws.rjobs[j];
+      const uint32_t c = static_cast<uint32_t>(radix_tiles<TILE>(jb.y > jb.x ? jb.y - jb.x : 0));
+      mn = min(mn, c);
+      mx = max(mx, c);
+    }
+    {
+      __shared__ uint32_t mm_s[2][NT / 32];
+      mn = __reduce_min_sync(0xFFFFFFFFu, mn);
+      mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+      if (lane == 0) {
+        mm_s[0][warp] = mn;
+        mm_s[1][warp] = mx;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int w = 0; w < NT / 32; ++w) {
+        mn = min(mn, mm_s[0][w]);
+        mx = max(mx, mm_s[1][w]);
+      }
+    }
+    // Every segment the same number of tiles: interleaved tile order.
+    interleave = nj > 1 && mn == mx;
     uint32_t total;
     uint32_t run = block_exclusive_add<NT>(sum, total, warp_s);
     for (int j = j0; j < j1; ++j) {
@@ -321,9 +351,15 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
     };
     auto fetch = [&](int64_t t, Tile &T) {
       T.t = t;
-      T.j = job_of(t);
+      int64_t k;
+      if (interleave) {
+        T.j = static_cast<int32_t>(t % nj);
+        k = t / nj;
+      } else {
+        T.j = job_of(t);
+        k = t - (local ? lpre[T.j] : ws.rtile_prefix[T.j]);
+      }
       const int4 jb = ws.rjobs[T.j];
-      const int64_t k = t - (local ? lpre[T.j] : ws.rtile_prefix[T.j]);
       const int64_t a = jb.x + k * TILE;
       T.cnt = static_cast<int>(min(static_cast<int64_t>(TILE), static_cast<int64_t>(jb.y) - a));
       const K *src = sp(jb.w).keys + a;
@@ -405,12 +441,14 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
   uint32_t copies = 0;  // bulk-copy phases of the mbarrier so far
   // Thread 0: describes tile t of pass d in *sl from its descriptor and its
   // segment's varying digits (loaded ahead by the caller).
-  auto describe = [&](int64_t t, const int4 &de, uint32_t varying, int d, RadixSlot *sl) {
+  auto describe = [&](int64_t t, const int4 &de, uint32_t varying, int32_t base, int d,
+                      RadixSlot *sl) {
     sl->t = t;
     sl->j = de.z;
     sl->a = de.x;
     sl->cnt = de.y;
     sl->k = de.w;
+    sl->w = base + de.w;
     sl->from_tmp = __popc(varying & ((1u << d) - 1u)) & 1;
     sl->active = (varying >> d) & 1u;
   };
@@ -438,7 +476,7 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       // async proxy.
       asm volatile("fence.proxy.async.global;" ::: "memory");
       const int4 de = ws.rtile_desc[blockIdx.x];
-      describe(blockIdx.x, de, ws.rdigits[de.z], d, &slot[0]);
+      describe(blockIdx.x, de, ws.rdigits[de.z], ws.rtile_prefix[de.z], d, &slot[0]);
       if (slot[0].active) issue(&slot[0], ws.rjobs[de.z].w);
     }
     __syncthreads();
@@ -452,7 +490,7 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       if (!cur.active) {  // the segment does not vary in this digit (uniform)
         __syncthreads();  // every thread has read slot[0]
         if (tid == 0 && tn < ntiles) {
-          describe(tn, nde, ws.rdigits[nde.z], d, &slot[0]);
+          describe(tn, nde, ws.rdigits[nde.z], ws.rtile_prefix[nde.z], d, &slot[0]);
           if (slot[0].active) issue(&slot[0], ws.rjobs[nde.z].w);
         }
         __syncthreads();
@@ -478,9 +516,11 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       // Thread 0: the next tile's segment, loaded under the ranking.
       uint32_t nvary = 0;
       int ninst = 0;
+      int32_t nbase = 0;
       if (tid == 0 && tn < ntiles) {
         nvary = ws.rdigits[nde.z];
         ninst = ws.rjobs[nde.z].w;
+        nbase = ws.rtile_prefix[nde.z];
       }
 
       // Keys of the tile, read from the staging buffer where needed: warp w
@@ -528,7 +568,7 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
         run += c;
       }
       const uint32_t tag_own = 2u * static_cast<uint32_t>(d + 1);
-      st_relaxed_u64(ws.rlook + cur.t * kRBuckets + b,
+      st_relaxed_u64(ws.rlook + static_cast<int64_t>(cur.w) * kRBuckets + b,
                      look_word(cur.k == 0 ? tag_own + 1u : tag_own, run));
       uint32_t tile_total;
       const uint32_t lstart = block_exclusive_add<NT>(run, tile_total, warp_s);
@@ -549,14 +589,14 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       }
       __syncthreads();  // staging buffers consumed
       if (tid == 0 && tn < ntiles) {
-        describe(tn, nde, nvary, d, &slot[0]);
+        describe(tn, nde, nvary, nbase, d, &slot[0]);
         if (slot[0].active) {
           fence_proxy_async();
           issue(&slot[0], ninst);
         }
       }
       // The counts of the segment's tiles before this one.
-      const uint32_t before = cur.k == 0 ? 0u : look_back_from(ws.rlook, cur.t, cur.k, b, run, d);
+      const uint32_t before = cur.k == 0 ? 0u : look_back_from(ws.rlook, cur.w, cur.k, b, run, d);
       const uint32_t bstart = ws.rhist[(static_cast<int64_t>(cur.j) * D + d) * kRBuckets + b];
       shift[b] = static_cast<int32_t>(bstart + before) - static_cast<int32_t>(lstart);
       __syncthreads();
