@@ -74,7 +74,7 @@ def parse_args():
     p.add_argument("--no-configs", action="store_true", help="skip the other workloads")
     p.add_argument("--no-served", action="store_true", help="skip the served-form stream")
     p.add_argument("--served-requests", type=int, default=100000)
-    p.add_argument("--served-rates", type=str, default="10000,20000,50000")
+    p.add_argument("--served-rates", type=str, default="5000,10000,50000")
     p.add_argument("--served-only", action="store_true",
                    help="run only the served-form request stream and print its JSON")
     return p.parse_args()

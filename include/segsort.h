@@ -342,7 +342,10 @@ int segsort_server_submit(segsort_server server, const uint32_t *h_keys,
                           int32_t nseg, uint32_t *h_keys_out, uint32_t *h_vals_out,
                           uint64_t *ticket);
 /* Blocks until the request is done; *latency_ms (optional) = completion
- * minus submission, host steady clock. */
+ * minus submission, host steady clock.  Wait once per ticket: the server
+ * keeps a request's record until its wait returns (a second wait on the
+ * ticket returns SEGSORT_ERR_INVALID_ARG), so a long-running server holds
+ * only the requests still in flight or not yet waited for. */
 int segsort_server_wait(segsort_server server, uint64_t ticket, double *latency_ms);
 /* Blocks until every submitted request is done. */
 int segsort_server_drain(segsort_server server);

@@ -27,6 +27,9 @@ constexpr int kMaxDevices = 64;
 // Tile-sort shape per key width: 4096-element chunks for 32-bit keys (256
 // threads x 16 words), 2048 for 64-bit keys (256 threads x 8 words).
 // Build-time tuning knobs (defaults are the measured best on GB300).
+#ifndef SEGSORT_TILE_NT32
+#define SEGSORT_TILE_NT32 256
+#endif
 #ifndef SEGSORT_TILE_KPT32
 #define SEGSORT_TILE_KPT32 16
 #endif
@@ -35,7 +38,8 @@ constexpr int kMaxDevices = 64;
 #endif
 template <typename K, bool PAIRS>
 struct TileFor {
-  using Cfg = TileConfig<K, PAIRS, 256, sizeof(K) == 4 ? SEGSORT_TILE_KPT32 : 8>;
+  using Cfg = TileConfig<K, PAIRS, sizeof(K) == 4 ? SEGSORT_TILE_NT32 : 256,
+                         sizeof(K) == 4 ? SEGSORT_TILE_KPT32 : 8>;
   static constexpr int kMinBlocks = SEGSORT_TILE_MINB;  // resident CTAs per SM the registers must allow
 };
 

@@ -41,6 +41,7 @@ struct Request {
   size_t bytes;  // device footprint charged against the budget
   Clock::time_point t_submit, t_done;
   bool done = false;
+  bool collected = false;  // segsort_server_wait has returned for it
   int status = SEGSORT_OK;
 };
 
@@ -75,7 +76,12 @@ struct segsort_server_s {
 
   std::mutex mu;
   std::condition_variable cv;
-  std::deque<Request> reqs;      // by ticket; deque keeps references stable
+  // Requests by ticket, from ticket `base` on: a request leaves the front
+  // once it is done and its wait has returned, so a long-running server
+  // holds only the requests still in flight or not yet waited for.  The
+  // deque keeps references to the others stable.
+  std::deque<Request> reqs;
+  uint64_t base = 0;
   std::deque<uint64_t> queue;    // submitted, not admitted
   uint64_t completed = 0;
   size_t in_flight = 0;          // admitted bytes not yet released
@@ -107,7 +113,7 @@ void CUDART_CB on_done(void *p) {
   const Clock::time_point now = Clock::now();
   std::lock_guard<std::mutex> lk(S->mu);
   for (uint64_t t : B->tickets) {
-    Request &r = S->reqs[t];
+    Request &r = S->reqs[t - S->base];
     r.t_done = now;
     r.done = true;
     S->stats.keys += r.n;
@@ -209,7 +215,7 @@ void worker_loop(segsort_server_s *S) {
     int64_t keys = 0;
     while (!S->queue.empty() &&
            (S->max_batch <= 0 || static_cast<int>(take.size()) < S->max_batch)) {
-      Request &r = S->reqs[S->queue.front()];
+      Request &r = S->reqs[S->queue.front() - S->base];
       // A batch closes once it holds max_batch_keys keys, so that the copies
       // of the next batch overlap its sort instead of waiting behind it.
       if (!take.empty() && keys + r.n > S->max_batch_keys) break;
@@ -248,7 +254,7 @@ void worker_loop(segsort_server_s *S) {
       if (S->stats.status == SEGSORT_OK) S->stats.status = rc;
       const Clock::time_point now = Clock::now();
       for (uint64_t t : raw->tickets) {
-        Request &r = S->reqs[t];
+        Request &r = S->reqs[t - S->base];
         r.status = rc;
         r.done = true;
         r.t_done = now;
@@ -320,7 +326,7 @@ int segsort_server_submit(segsort_server S, const uint32_t *h_keys, const uint32
   r.t_submit = Clock::now();
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->stop) return SEGSORT_ERR_INVALID_ARG;
-  *ticket = S->reqs.size();
+  *ticket = S->base + S->reqs.size();
   S->reqs.push_back(r);
   S->queue.push_back(*ticket);
   S->cv.notify_all();
@@ -330,18 +336,26 @@ int segsort_server_submit(segsort_server S, const uint32_t *h_keys, const uint32
 int segsort_server_wait(segsort_server S, uint64_t ticket, double *latency_ms) {
   if (S == nullptr) return SEGSORT_ERR_INVALID_ARG;
   std::unique_lock<std::mutex> lk(S->mu);
-  if (ticket >= S->reqs.size()) return SEGSORT_ERR_INVALID_ARG;
-  S->cv.wait(lk, [&] { return S->reqs[ticket].done; });
-  const Request &r = S->reqs[ticket];
+  if (ticket < S->base || ticket >= S->base + S->reqs.size() ||
+      S->reqs[ticket - S->base].collected)
+    return SEGSORT_ERR_INVALID_ARG;  // unknown, or already waited for
+  S->cv.wait(lk, [&] { return S->reqs[ticket - S->base].done; });
+  Request &r = S->reqs[ticket - S->base];
   if (latency_ms)
     *latency_ms = std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count();
-  return r.status;
+  const int status = r.status;
+  r.collected = true;
+  while (!S->reqs.empty() && S->reqs.front().done && S->reqs.front().collected) {
+    S->reqs.pop_front();
+    ++S->base;
+  }
+  return status;
 }
 
 int segsort_server_drain(segsort_server S) {
   if (S == nullptr) return SEGSORT_ERR_INVALID_ARG;
   std::unique_lock<std::mutex> lk(S->mu);
-  S->cv.wait(lk, [&] { return S->completed == S->reqs.size(); });
+  S->cv.wait(lk, [&] { return S->completed == S->base + S->reqs.size(); });
   return S->stats.status;
 }
 

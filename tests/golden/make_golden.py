@@ -23,13 +23,14 @@ from __future__ import annotations
 import importlib.util
 import subprocess
 import sys
+import os
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = Path("/root/reference")
+REF = Path(os.environ.get("SEGSORT_REF_DIR", "/root/reference"))
 sys.path.insert(0, str(REPO))
 
 from oracle import oracle as O  # noqa: E402

@@ -119,3 +119,33 @@ def test_served_one_request_per_batch(pkg, cuda, inst, oracle):
     for (keys, vals, off), (k, v) in zip(reqs, got):
         ek, ev = oracle.segsort_numpy(keys, off, vals)
         assert np.array_equal(k, ek) and np.array_equal(v, ev)
+
+
+def test_records_are_released_once_waited(pkg, cuda, inst):
+    """Each ticket is waited for once; the server forgets a request after its
+    wait returns, so a second wait on it is refused, while later tickets keep
+    working after many earlier ones have been released."""
+    import ctypes
+    torch = cuda
+    reqs = _requests(inst, 30, seed=301)
+    bufs = [(_pinned(torch, keys), _pinned(torch, vals), _pinned(torch, off),
+             torch.zeros(len(keys), dtype=torch.int32, pin_memory=True),
+             torch.zeros(len(keys), dtype=torch.int32, pin_memory=True))
+            for keys, vals, off in reqs]
+    srv = pkg.Server(1 << 33)
+    try:
+        for rnd in range(3):  # three rounds of submit-all / wait-all
+            tickets = [srv.submit(*[b.numpy() for b in bb]) for bb in bufs]
+            for t in tickets:
+                srv.wait(t)
+            for t in tickets[:3]:
+                rc = pkg.lib().segsort_server_wait(srv._h, t, None)
+                assert rc == pkg.SEGSORT_ERR_INVALID_ARG
+            for (keys, vals, off), bb in zip(reqs, bufs):
+                ek, ev = _plain_alone(pkg, torch, keys, vals, off)
+                assert np.array_equal(bb[3].numpy().view(np.uint32), ek)
+                assert np.array_equal(bb[4].numpy().view(np.uint32), ev)
+        st = srv.stats()
+        assert st["requests"] == 90 and st["status"] == pkg.SEGSORT_OK
+    finally:
+        srv.close()
