@@ -337,6 +337,34 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
         if rc != 0:
             raise pkg.SegsortError(rc, "segsort_batch_plan_launch")
 
+    def group_times() -> dict:
+        """Per key type: a plan of that type's instances alone, and the same
+        instances as plain calls (median ms)."""
+        out = {}
+        for kt in sorted({r["spec"]["key_type"] for r in rows}):
+            sub = [i for i, r in enumerate(rows) if r["spec"]["key_type"] == kt]
+            sub_items = (pkg.BatchItem * len(sub))(*[items[i] for i in sub])
+            gp = ctypes.c_void_p()
+            if L.segsort_batch_plan_create(sub_items, len(sub), ctypes.byref(gp)) != 0:
+                continue
+            try:
+                t_g = _timed(stream, lambda: L.segsort_batch_plan_launch(gp, st), restore, 1, 3)
+            finally:
+                L.segsort_batch_plan_destroy(gp)
+
+            def plain_sub():
+                for i in sub:
+                    r, sp = rows[i], rows[i]["spec"]
+                    getattr(L, f"segsort_pairs_{sp['key_type']}")(
+                        r["k"].data_ptr(), r["v"].data_ptr(), sp["n"], r["off"].data_ptr(),
+                        r["off"].numel() - 1, st)
+            t_p = _timed(stream, plain_sub, restore, 1, 3)
+            keys = sum(rows[i]["spec"]["n"] for i in sub)
+            out[kt] = {"instances": len(sub), "keys": keys,
+                       "plan_ms": round(statistics.median(t_g), 4),
+                       "plain_ms": round(statistics.median(t_p), 4)}
+        return out
+
     try:
         t_plain = _timed(stream, plain, restore, warmup, steps)
         ref = [(r["k"].clone(), r["v"].clone()) for r in rows]
@@ -345,6 +373,7 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
         identical = all(torch.equal(r["k"], k) and torch.equal(r["v"], v)
                         for r, (k, v) in zip(rows, ref))
         ws = L.segsort_batch_plan_workspace_bytes(plan)
+        groups = group_times()
     finally:
         L.segsort_batch_plan_destroy(plan)
     if pkg.device_status() != 0:
@@ -364,7 +393,7 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
         "speedup_plan_vs_plain": round(med["plain"] / med["plan"], 3),
         "plan_p99_ms": round(float(np.percentile(t_plan, 99)), 4),
         "identical_to_plain": identical, "plan_workspace_bytes": ws, "steps": steps,
-        "tuned_merge_ctas_per_sm": tuned.value,
+        "tuned_merge_ctas_per_sm": tuned.value, "by_key_type": groups,
         "launches": {"plain": 3 * len(specs), "plan_graph": 3 * len(types)},
     }
 

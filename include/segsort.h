@@ -390,6 +390,32 @@ int segsort_pool_bytes(int *created, uint64_t *used);
 int segsort_set_param(int param, int64_t value);
 int segsort_get_param(int param, int64_t *value);
 
+/* Autotuner of plain calls (no counterpart in the reference).
+ * segsort_tune_pairs_u32 sorts the given problem like segsort_pairs_u32, but
+ * first measures it -- on copies of the inputs, each route timed three times
+ * after one untimed call -- under candidate routes: the radix threshold
+ * (4096, 2^15, 2^17, off), the streamed-tile kernel (never, always) and the
+ * long-segment kernel's resident CTAs per SM (1, 2, all), one after the
+ * other, keeping a candidate that is at least 2% faster.  The chosen route is
+ * returned (optional outputs), recorded for the problem's class in this
+ * process, and appended to cache_path (optional) as a line
+ *   plain k<key bytes> n<log2 n> len<log2 (n / nseg)> <radix> <stream> <ctas>
+ * Later plain calls of that class (any key type of the same width) take the
+ * recorded route.  segsort_tune_load reads such lines from a file into the
+ * process's table (returns how many, or SEGSORT_ERR_INVALID_ARG when the
+ * file cannot be read; lines of other formats are skipped);
+ * segsort_tune_clear empties it; segsort_tune_lookup returns 1 and the
+ * route recorded for a class, 0 when there is none.  The tuner synchronises
+ * `stream` and allocates from the library's pool; the others are host-only. */
+int segsort_tune_pairs_u32(uint32_t *d_keys, uint32_t *d_vals, int64_t n,
+                           const int32_t *d_offsets, int32_t nseg, segsort_stream_t stream,
+                           const char *cache_path, int64_t *radix_min,
+                           int64_t *stream_max_avg, int32_t *merge_ctas_per_sm);
+int segsort_tune_load(const char *cache_path);
+void segsort_tune_clear(void);
+int segsort_tune_lookup(int key_bytes, int64_t n, int32_t nseg, int64_t *radix_min,
+                        int64_t *stream_max_avg, int32_t *merge_ctas_per_sm);
+
 /* Self-test of the bounded device waits (no counterpart in the reference).
  * Launches a small kernel on a stream of its own whose wait can never
  * complete -- which = 0: a grid barrier that one of its two CTAs never

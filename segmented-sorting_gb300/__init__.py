@@ -90,6 +90,12 @@ SIGNATURES = {
     "segsort_server_destroy": ([_P], None),
     "segsort_pool_bytes": ([ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "segsort_set_param": ([ctypes.c_int, _I64], ctypes.c_int),
+    "segsort_tune_pairs_u32": ([_P, _P, _I64, _P, _I32, _P, ctypes.c_char_p, ctypes.POINTER(_I64),
+                                ctypes.POINTER(_I64), ctypes.POINTER(_I32)], ctypes.c_int),
+    "segsort_tune_load": ([ctypes.c_char_p], ctypes.c_int),
+    "segsort_tune_clear": ([], None),
+    "segsort_tune_lookup": ([ctypes.c_int, _I64, _I32, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                             ctypes.POINTER(_I32)], ctypes.c_int),
     "segsort_get_param": ([ctypes.c_int, ctypes.POINTER(_I64)], ctypes.c_int),
     "segsort_selftest_wait_timeout": ([ctypes.c_int], ctypes.c_int),
     "segsort_device_status": ([ctypes.c_int], ctypes.c_int),

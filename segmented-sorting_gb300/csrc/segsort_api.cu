@@ -38,17 +38,13 @@ cudaEvent_t prof_event(cudaStream_t stream) {
   return e;
 }
 
-// Problems whose average segment is at most this long take the half-tile
-// classify and the streamed tile kernel (measured on GB300 over 2^24 pairs:
-// both faster up to 32, slower from 64).  Run-time parameter
-// (segsort_set_param); a huge value sends every multi-tile problem through
-// them.
-std::atomic<int64_t> g_stream_max_avg{32};
-
 // ---------------------------------------------------------------------------
+// One plain call.  forced: the route to take (the tuner's trials); null: the
+// call's own (route_for).
 template <typename K, bool PAIRS>
 int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_t nseg,
-              bool heads, void *ws, size_t ws_bytes, cudaStream_t stream) {
+              bool heads, void *ws, size_t ws_bytes, cudaStream_t stream,
+              const CallRoute *forced = nullptr) {
   if (n < 0 || nseg < 0) return SEGSORT_ERR_INVALID_ARG;
   if (n == 0 || nseg == 0) return SEGSORT_OK;
   if (keys == nullptr || offsets == nullptr || (PAIRS && vals == nullptr))
@@ -61,6 +57,8 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   if (S == nullptr) return SEGSORT_ERR_CUDA;
 
   const Offsets off{offsets, nseg, heads ? 1 : 0, n};
+  CallRoute R = forced != nullptr ? *forced : route_for<K>(n, nseg);
+  R.radix_min = clamp_radix_min<K>(R.radix_min);
 
   // ---- shapes ---------------------------------------------------------------
   using Cfg = typename TileFor<K, PAIRS>::Cfg;
@@ -89,7 +87,8 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // ---- workspace ----------------------------------------------------------------
   // A caller's workspace is sized for every radix threshold
   // (segsort_workspace_bytes); the library's own is sized for the current one.
-  const WsLayout L = ws != nullptr ? layout_any_threshold<K, PAIRS>(n) : layout_for<K, PAIRS>(n);
+  const WsLayout L =
+      ws != nullptr ? layout_any_threshold<K, PAIRS>(n) : layout_for<K, PAIRS>(n, R.radix_min);
   bool owned = false;
   unsigned char *base = static_cast<unsigned char *>(ws);
   if (base == nullptr) {
@@ -106,7 +105,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   }
 
   LargeWs<K> W = ws_views<K, PAIRS>(base, L);
-  W.radix_min = std::max<int64_t>(L.radix_min, radix_min_for<K>());
+  W.radix_min = std::max<int64_t>(L.radix_min, R.radix_min);
 
   int rc = SEGSORT_OK;
   do {
@@ -119,7 +118,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // otherwise one thread per segment boundary (work ~ nseg, fewer rounds
     // of dependent loads).  The two write the same map and jobs.
     const bool short_avg =
-        n <= g_stream_max_avg.load(std::memory_order_relaxed) * static_cast<int64_t>(nseg);
+        R.stream_max_avg > 0 && n <= R.stream_max_avg * static_cast<int64_t>(nseg);
     if (short_avg) {
       const unsigned blocks =
           static_cast<unsigned>((W.halves + kClassifyWarps) / kClassifyWarps);  // halves + 1 entries
@@ -176,9 +175,10 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // All resident CTAs, but no more than one per merge item of the whole
     // problem: small calls then leave the rest of the GPU to other work.
     const int mo = occupancy(merge_kernel, kMThreads, MS::kBytes, merge_occ, dev);
+    const int per_sm = R.merge_per_sm > 0 ? std::min(R.merge_per_sm, mo) : mo;
     const int64_t items = n / MergeShape<K>::T + 1;
     const unsigned merge_grid =
-        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(mo) * S->sms, items));
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(per_sm) * S->sms, items));
     if (prof) rec.l0 = prof_event(stream);
     {
       SingleSpace<K> sp{keys, vals, W.tmp_keys, W.tmp_vals};
@@ -265,6 +265,112 @@ __global__ void selftest_mbar_kernel() {
     mbar_arrive_expect_tx(&bar, 16);
     if (!mbar_wait(&bar, 0, kSelftestSpins)) raise_status(kStatusTimeout);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Tuner of plain calls: the median of three timed calls (after an untimed
+// one) of the sort with route R, each on a fresh copy of the saved inputs.
+template <typename K, bool PAIRS>
+int time_route(K *keys, uint32_t *vals, const K *k0, const uint32_t *v0, int64_t n,
+               const int32_t *offsets, int32_t nseg, cudaStream_t stream, const CallRoute &R,
+               cudaEvent_t a, cudaEvent_t b, float *ms) {
+  float t[3] = {0.f, 0.f, 0.f};
+  for (int r = -1; r < 3; ++r) {
+    if (cudaMemcpyAsync(keys, k0, n * sizeof(K), cudaMemcpyDeviceToDevice, stream) != cudaSuccess ||
+        (PAIRS && cudaMemcpyAsync(vals, v0, n * 4, cudaMemcpyDeviceToDevice, stream) != cudaSuccess) ||
+        cudaEventRecord(a, stream) != cudaSuccess)
+      return SEGSORT_ERR_CUDA;
+    const int rc = sort_impl<K, PAIRS>(keys, vals, n, offsets, nseg, false, nullptr, 0, stream, &R);
+    if (rc != SEGSORT_OK) return rc;
+    if (cudaEventRecord(b, stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess)
+      return SEGSORT_ERR_CUDA;
+    if (r >= 0 && cudaEventElapsedTime(&t[r], a, b) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  }
+  std::sort(t, t + 3);
+  *ms = t[1];
+  return SEGSORT_OK;
+}
+
+// Coordinate search over the route of one problem: the radix threshold, then
+// the streamed-tile threshold, then the long-segment kernel's CTAs per SM; a
+// candidate replaces the best so far when it is at least 2% faster.  On
+// return the caller's buffers hold the problem sorted with the chosen route.
+template <typename K, bool PAIRS>
+int tune_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_t nseg,
+              cudaStream_t stream, CallRoute *best) {
+  if (n < 0 || nseg < 0) return SEGSORT_ERR_INVALID_ARG;
+  *best = route_for<K>(n, nseg);
+  if (n == 0 || nseg == 0) return SEGSORT_OK;
+  if (keys == nullptr || offsets == nullptr || (PAIRS && vals == nullptr))
+    return SEGSORT_ERR_INVALID_ARG;
+  if (n >= (int64_t{1} << 30)) return SEGSORT_ERR_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SEGSORT_ERR_CUDA;
+  DeviceState *S = device_state(dev);
+  cudaMemPool_t pool = S ? device_pool(*S, dev) : nullptr;
+  const size_t kbytes = static_cast<size_t>(n) * sizeof(K), vbytes = PAIRS ? n * 4 : 0;
+  unsigned char *saved = nullptr;
+  if (pool == nullptr ||
+      cudaMallocFromPoolAsync(reinterpret_cast<void **>(&saved), align256(kbytes) + vbytes + 256,
+                              pool, stream) != cudaSuccess) {
+    cudaGetLastError();
+    return SEGSORT_ERR_NO_MEMORY;
+  }
+  K *k0 = reinterpret_cast<K *>(saved);
+  uint32_t *v0 = reinterpret_cast<uint32_t *>(saved + align256(kbytes));
+  cudaEvent_t a = nullptr, b = nullptr;
+  int rc = SEGSORT_OK;
+  if (cudaMemcpyAsync(k0, keys, kbytes, cudaMemcpyDeviceToDevice, stream) != cudaSuccess ||
+      (PAIRS && cudaMemcpyAsync(v0, vals, vbytes, cudaMemcpyDeviceToDevice, stream) != cudaSuccess) ||
+      cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+    rc = SEGSORT_ERR_CUDA;
+  float best_ms = 0.f;
+  if (rc == SEGSORT_OK)
+    rc = time_route<K, PAIRS>(keys, vals, k0, v0, n, offsets, nseg, stream, *best, a, b, &best_ms);
+  auto consider = [&](CallRoute R) {
+    float ms = 0.f;
+    if (rc != SEGSORT_OK) return;
+    rc = time_route<K, PAIRS>(keys, vals, k0, v0, n, offsets, nseg, stream, R, a, b, &ms);
+    if (rc == SEGSORT_OK && ms < 0.98f * best_ms) {
+      *best = R;
+      best_ms = ms;
+    }
+  };
+  const CallRoute start = *best;
+  for (int64_t v : {kRadixMinFloor, int64_t{1} << 15, int64_t{1} << 17, int64_t{1} << 30}) {
+    CallRoute R = *best;
+    R.radix_min = clamp_radix_min<K>(v);
+    if (R.radix_min != start.radix_min) consider(R);
+  }
+  for (int64_t v : {int64_t{0}, int64_t{1} << 30}) {  // streamed tile kernel: never, always
+    CallRoute R = *best;
+    R.stream_max_avg = v;
+    if ((n <= v * static_cast<int64_t>(nseg)) != (n <= start.stream_max_avg * static_cast<int64_t>(nseg)))
+      consider(R);
+  }
+  for (int32_t v : {1, 2}) {
+    CallRoute R = *best;
+    R.merge_per_sm = v;
+    consider(R);
+  }
+  // The caller's buffers end sorted with the chosen route.
+  if (rc == SEGSORT_OK &&
+      (cudaMemcpyAsync(keys, k0, kbytes, cudaMemcpyDeviceToDevice, stream) != cudaSuccess ||
+       (PAIRS && cudaMemcpyAsync(vals, v0, vbytes, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)))
+    rc = SEGSORT_ERR_CUDA;
+  if (rc == SEGSORT_OK)
+    rc = sort_impl<K, PAIRS>(keys, vals, n, offsets, nseg, false, nullptr, 0, stream, best);
+  if (cudaFreeAsync(saved, stream) != cudaSuccess && rc == SEGSORT_OK) rc = SEGSORT_ERR_CUDA;
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  return rc;
+}
+
+// Records a route for a class in the process's table.
+void record_route(uint32_t cls, const CallRoute &R) {
+  std::unique_lock<std::shared_mutex> lk(g_tuned.mu);
+  g_tuned.by_class[cls] = R;
+  g_tuned.any.store(true, std::memory_order_release);
 }
 
 // The look-back of tile 1 of a segment whose tile 0 never publishes.
@@ -419,6 +525,73 @@ int segsort_get_param(int param, int64_t *value) {
     default:
       return SEGSORT_ERR_INVALID_ARG;
   }
+}
+
+int segsort_tune_pairs_u32(uint32_t *k, uint32_t *v, int64_t n, const int32_t *o, int32_t ns,
+                           segsort_stream_t s, const char *cache_path, int64_t *radix_min,
+                           int64_t *stream_max_avg, int32_t *merge_ctas_per_sm) {
+  using namespace segsort;
+  CallRoute R{};
+  const int rc = tune_impl<uint32_t, true>(k, v, n, o, ns, SEGSORT_ST(s), &R);
+  if (rc != SEGSORT_OK) return rc;
+  if (n > 0 && ns > 0) {
+    const uint32_t cls = route_class(4, n, ns);
+    record_route(cls, R);
+    if (cache_path != nullptr) {
+      if (FILE *f = std::fopen(cache_path, "a")) {
+        std::fprintf(f, "plain k%u n%u len%u %lld %lld %d\n", cls >> 16, (cls >> 8) & 255u, cls & 255u,
+                     static_cast<long long>(R.radix_min), static_cast<long long>(R.stream_max_avg),
+                     R.merge_per_sm);
+        std::fclose(f);
+      }
+    }
+  }
+  if (radix_min) *radix_min = R.radix_min;
+  if (stream_max_avg) *stream_max_avg = R.stream_max_avg;
+  if (merge_ctas_per_sm) *merge_ctas_per_sm = R.merge_per_sm;
+  return SEGSORT_OK;
+}
+
+int segsort_tune_load(const char *cache_path) {
+  using namespace segsort;
+  if (cache_path == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  FILE *f = std::fopen(cache_path, "r");
+  if (f == nullptr) return SEGSORT_ERR_INVALID_ARG;
+  char line[256];
+  int loaded = 0;
+  while (std::fgets(line, sizeof(line), f)) {
+    unsigned kb = 0, lgn = 0, lgl = 0;
+    long long radix = 0, stream = 0;
+    int merge = 0;
+    if (std::sscanf(line, "plain k%u n%u len%u %lld %lld %d", &kb, &lgn, &lgl, &radix, &stream,
+                    &merge) != 6)
+      continue;  // another tuner's line
+    if ((kb != 4 && kb != 8) || lgn > 40 || lgl > 40 || radix < 0 || stream < 0 || merge < 0 ||
+        merge > 64)
+      continue;
+    record_route((kb << 16) | (lgn << 8) | lgl, CallRoute{radix, stream, merge});
+    ++loaded;
+  }
+  std::fclose(f);
+  return loaded;
+}
+
+void segsort_tune_clear(void) {
+  using namespace segsort;
+  std::unique_lock<std::shared_mutex> lk(g_tuned.mu);
+  g_tuned.by_class.clear();
+  g_tuned.any.store(false, std::memory_order_release);
+}
+
+int segsort_tune_lookup(int key_bytes, int64_t n, int32_t nseg, int64_t *radix_min,
+                        int64_t *stream_max_avg, int32_t *merge_ctas_per_sm) {
+  using namespace segsort;
+  CallRoute R;
+  if (!tuned_route(route_class(key_bytes, n, nseg), &R)) return 0;
+  if (radix_min) *radix_min = R.radix_min;
+  if (stream_max_avg) *stream_max_avg = R.stream_max_avg;
+  if (merge_ctas_per_sm) *merge_ctas_per_sm = R.merge_per_sm;
+  return 1;
 }
 
 int segsort_selftest_wait_timeout(int which) {

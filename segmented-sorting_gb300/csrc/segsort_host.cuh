@@ -8,6 +8,8 @@
 #include <atomic>
 #include <cstdint>
 #include <mutex>
+#include <shared_mutex>
+#include <unordered_map>
 
 #include <cuda_runtime.h>
 
@@ -63,9 +65,73 @@ inline std::atomic<int64_t> g_radix_min32{int64_t{1} << 15};
 inline std::atomic<int64_t> g_radix_min64{int64_t{1} << 18};
 
 template <typename K>
-inline int64_t radix_min_for() {
-  const int64_t v = (sizeof(K) == 8 ? g_radix_min64 : g_radix_min32).load(std::memory_order_relaxed);
+inline int64_t clamp_radix_min(int64_t v) {
   return std::max<int64_t>(std::max<int64_t>(v, kRadixMinFloor), tile_cap<K>());
+}
+
+template <typename K>
+inline int64_t radix_min_for() {
+  return clamp_radix_min<K>(
+      (sizeof(K) == 8 ? g_radix_min64 : g_radix_min32).load(std::memory_order_relaxed));
+}
+
+// Problems whose average segment is at most this long take the half-tile
+// classify and the streamed tile kernel (measured on GB300 over 2^24 pairs:
+// both faster up to 32, slower from 64).  Run-time parameter
+// (segsort_set_param); a huge value sends every multi-tile problem through
+// them.
+inline std::atomic<int64_t> g_stream_max_avg{32};
+
+// ---------------------------------------------------------------------------
+// Route of one plain call: the radix threshold, the streamed-tile threshold
+// and the resident CTAs per SM of the long-segment kernel (0: as many as
+// fit).  From the process-wide parameters, unless the tuner recorded a route
+// for the call's class (segsort_tune_pairs_u32 / segsort_tune_load).
+struct CallRoute {
+  int64_t radix_min;
+  int64_t stream_max_avg;
+  int32_t merge_per_sm;
+};
+
+// Class of a plain call: key width, log2 of n, log2 of the average segment.
+inline uint32_t route_class(int key_bytes, int64_t n, int32_t nseg) {
+  auto lg = [](int64_t x) {
+    int l = 0;
+    while (x > 1) {
+      x >>= 1;
+      ++l;
+    }
+    return static_cast<uint32_t>(l);
+  };
+  const int64_t avg = nseg > 0 ? std::max<int64_t>(1, n / nseg) : 1;
+  return (static_cast<uint32_t>(key_bytes) << 16) | (lg(n) << 8) | lg(avg);
+}
+
+struct TunedRoutes {
+  std::shared_mutex mu;
+  std::unordered_map<uint32_t, CallRoute> by_class;
+  std::atomic<bool> any{false};
+};
+inline TunedRoutes g_tuned;
+
+inline bool tuned_route(uint32_t cls, CallRoute *r) {
+  if (!g_tuned.any.load(std::memory_order_acquire)) return false;
+  std::shared_lock<std::shared_mutex> lk(g_tuned.mu);
+  const auto it = g_tuned.by_class.find(cls);
+  if (it == g_tuned.by_class.end()) return false;
+  *r = it->second;
+  return true;
+}
+
+template <typename K>
+inline CallRoute route_for(int64_t n, int32_t nseg) {
+  CallRoute r{radix_min_for<K>(), g_stream_max_avg.load(std::memory_order_relaxed), 0};
+  CallRoute t;
+  if (tuned_route(route_class(static_cast<int>(sizeof(K)), n, nseg), &t)) {
+    r = t;
+    r.radix_min = clamp_radix_min<K>(r.radix_min);
+  }
+  return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -135,11 +201,10 @@ constexpr WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t 
   return L;
 }
 
-// The layout a call of n elements uses, for the current radix threshold.
+// The layout a call of n elements uses, for its radix threshold.
 template <typename K, bool PAIRS>
-inline WsLayout layout_for(int64_t n) {
-  return make_layout(n, sizeof(K), PAIRS ? 4 : 0, tile_cap<K>(), MergeShape<K>::T, -1,
-                     radix_min_for<K>());
+inline WsLayout layout_for(int64_t n, int64_t radix_min) {
+  return make_layout(n, sizeof(K), PAIRS ? 4 : 0, tile_cap<K>(), MergeShape<K>::T, -1, radix_min);
 }
 
 // A layout that serves every radix threshold (caller-sized workspaces).

@@ -217,3 +217,32 @@ def test_batch_tune_rejects_a_missing_plan(pkg):
     L = pkg.lib()
     k = ctypes.c_int32()
     assert L.segsort_batch_plan_tune(None, None, None, ctypes.byref(k)) == pkg.SEGSORT_ERR_INVALID_ARG
+
+
+def test_tuned_route_table(pkg, tmp_path):
+    """segsort_tune_load / _lookup / _clear are host-only: the cache file's
+    plain-call lines become the routes of their classes; other lines are
+    skipped."""
+    L = pkg.lib()
+    cache = tmp_path / "routes.txt"
+    cache.write_text("t1-n24-max20-len10 3\n"             # a batch-plan line
+                     "plain k4 n24 len10 32768 32 2\n"
+                     "plain k8 n20 len4 4096 0 0\n"
+                     "plain k4 n24 len10 131072 0 1\n"     # a later line wins
+                     "garbage\n")
+    L.segsort_tune_clear()
+    r, st, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+    assert L.segsort_tune_lookup(4, 1 << 24, 1 << 14, ctypes.byref(r), ctypes.byref(st),
+                                 ctypes.byref(c)) == 0
+    assert L.segsort_tune_load(str(cache).encode()) == 3
+    assert L.segsort_tune_lookup(4, 1 << 24, 1 << 14, ctypes.byref(r), ctypes.byref(st),
+                                 ctypes.byref(c)) == 1
+    assert (r.value, st.value, c.value) == (131072, 0, 1)
+    # the class is log2 n and log2 (n / nseg): 2^24 + 5 keys in 2^14 segments share it
+    assert L.segsort_tune_lookup(4, (1 << 24) + 5, 1 << 14, None, None, None) == 1
+    assert L.segsort_tune_lookup(8, (1 << 20) + 100, 1 << 16, ctypes.byref(r), None, None) == 1
+    assert r.value == 4096
+    assert L.segsort_tune_lookup(4, 1 << 23, 1 << 14, None, None, None) == 0
+    assert L.segsort_tune_load(str(tmp_path / "missing").encode()) == pkg.SEGSORT_ERR_INVALID_ARG
+    L.segsort_tune_clear()
+    assert L.segsort_tune_lookup(4, 1 << 24, 1 << 14, None, None, None) == 0
