@@ -1,0 +1,334 @@
+// Bucket sort of a tile chunk: the first try for every chunk the tile kernel
+// sorts, with the comparison sort of tile_sort.cuh as the fallback.
+//
+// A chunk holds whole segments (or one CAP-run of a long segment).  Every
+// key of segment [s, t) (chunk positions) is sent to the bucket
+//     s + floor(x * (t - s) / 2^W),
+// x its order bits shifted left past the bits that are equal over the whole
+// chunk (W = the bit width), so the buckets of a segment are its own
+// positions, in key order: a key in a lower bucket is smaller than every key
+// in a higher one.  With keys spread over their range the buckets hold about
+// one key each.  One shared-memory atomic per key counts the buckets (and
+// gives each key a slot in its bucket, in no particular order), an exclusive
+// scan turns the counts into bucket starts, the keys -- as (order bits,
+// chunk index) words, the tile sort's composite words without the segment
+// field -- and the values are scattered to their buckets, and every key's
+// final position is its bucket's start plus the number of the bucket's words
+// below its own: the stable order.  A thread per slot keeps a warp's stores
+// on consecutive positions.
+//
+// The ranking costs the sum of the squared bucket sizes.  When that sum is
+// above kBucketSkew * m, or a bucket holds more than kBucketMaxSize keys (few
+// distinct keys, skewed keys, keys of a segment packed in a narrow range),
+// the function writes nothing and returns false, and the caller sorts the
+// chunk with the comparison sort.  A chunk whose keys are all equal is
+// already in its stable order (copied when the result goes elsewhere).
+//
+// The result is the same as the comparison sort's, bit for bit: both give the
+// stable order of each segment, which is unique.  The reference sorts these
+// lengths with per-length-bin register networks and block merges
+// (src/bb_segsort/bb_segsort.h:71-164); this is a different method with the
+// same output.
+#pragma once
+
+#include "tile_sort.cuh"
+
+namespace segsort {
+
+constexpr uint32_t kBucketSkew = 3;      // sum of squared bucket sizes <= 3 m
+constexpr uint32_t kBucketMaxSize = 24;  // largest bucket a thread ranks alone
+// Buckets up to this size are ranked by an unrolled loop of this many
+// compares; with about one key per bucket (Poisson sizes) a larger bucket
+// is rare.
+constexpr int kBucketUnroll = 6;
+
+template <typename Bits>
+__device__ __forceinline__ uint32_t bucket_scale(Bits x, uint32_t len);
+template <>
+__device__ __forceinline__ uint32_t bucket_scale<uint32_t>(uint32_t x, uint32_t len) {
+  return __umulhi(x, len);
+}
+template <>
+__device__ __forceinline__ uint32_t bucket_scale<uint64_t>(uint64_t x, uint32_t len) {
+  return static_cast<uint32_t>(__umul64hi(x, static_cast<uint64_t>(len)));
+}
+
+template <typename Bits>
+__device__ __forceinline__ int leading_zeros(Bits x);
+template <>
+__device__ __forceinline__ int leading_zeros<uint32_t>(uint32_t x) { return __clz(x); }
+template <>
+__device__ __forceinline__ int leading_zeros<uint64_t>(uint64_t x) {
+  return __clzll(static_cast<long long>(x));
+}
+
+// Shared memory of the bucket sort (dynamic; the tile kernel's buffer is
+// sized for the larger of this and the comparison sort's layout).
+template <typename Cfg, bool PAIRS>
+struct BucketLayout {
+  static constexpr int CAP = Cfg::CAP;
+  static constexpr size_t kWords = 0;                                        // Word[CAP]
+  static constexpr size_t kVals = kWords + CAP * sizeof(typename Cfg::Word);  // uint32[CAP]
+  static constexpr size_t kBkt = kVals + (PAIRS ? CAP * sizeof(uint32_t) : 0);  // uint16[CAP]
+  static constexpr size_t kCnt = (kBkt + CAP * sizeof(uint16_t) + 15) / 16 * 16;
+  // Bucket counters, then starts: one padding word per 32 keeps the blocked
+  // scan free of bank conflicts; one past the last bucket holds m.
+  static constexpr int kCntSlots = CAP + CAP / 32 + 2;
+  static constexpr size_t kBytes = kCnt + kCntSlots * sizeof(uint32_t);
+  static __device__ __forceinline__ int cslot(int b) { return b + (b >> 5); }
+};
+
+template <typename Cfg, bool PAIRS>
+constexpr size_t tile_smem_bytes() {
+  return Cfg::kSmemBytes > BucketLayout<Cfg, PAIRS>::kBytes ? Cfg::kSmemBytes
+                                                             : BucketLayout<Cfg, PAIRS>::kBytes;
+}
+
+// Sorts chunk C by buckets, or returns false (uniformly over the CTA) having
+// written nothing.  Every thread of the CTA calls it; hb is the tile
+// kernel's head bitmask (CAP / 32 words), warp_s its scan scratch.  Starts and
+// ends with a barrier, so it may follow and precede any other use of the
+// shared memory.
+template <typename Cfg, bool PAIRS, typename K>
+__device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint32_t *vals,
+                                               const Offsets &off, K *tmp_keys,
+                                               uint32_t *tmp_vals, unsigned char *smem,
+                                               uint32_t *hb, int *warp_s) {
+  using Ord = typename Cfg::Ord;
+  using Bits = typename Cfg::Bits;
+  using WT = typename Cfg::WT;
+  using Word = typename Cfg::Word;
+  using BL = BucketLayout<Cfg, PAIRS>;
+  constexpr int NT = Cfg::NT;
+  constexpr int CAP = Cfg::CAP;
+  constexpr int IPT = CAP / NT;
+  constexpr int NW = NT / 32;
+  constexpr int HW = CAP / 32;  // head words
+  constexpr int WPL = HW / 32;  // head words per lane of warp 0
+  static_assert(HW % 32 == 0, "head words split evenly over a warp");
+  static_assert(CAP <= 32768, "bucket and slot share a 32-bit word");
+  __shared__ uint32_t red_s[4][NW];
+  __shared__ int32_t hprev[HW], hnext[HW];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const ChunkIO<K, PAIRS> io(C, keys, vals, tmp_keys, tmp_vals);
+  const int m = C.m;
+  const bool multi = C.hi - C.lo > 1;
+  Word *SW = reinterpret_cast<Word *>(smem + BL::kWords);
+  uint32_t *SV = reinterpret_cast<uint32_t *>(smem + BL::kVals);
+  uint16_t *SB = reinterpret_cast<uint16_t *>(smem + BL::kBkt);
+  uint32_t *CN = reinterpret_cast<uint32_t *>(smem + BL::kCnt);
+
+  // ---- keys and values to registers (position q * NT + tid); the chunk's
+  // AND and OR of the order bits ------------------------------------------------
+  Bits kb[IPT];
+  uint32_t kv[IPT];
+  Bits band = ~Bits(0), bor = 0;
+#pragma unroll
+  for (int q = 0; q < IPT; ++q) {
+    const int i = q * NT + tid;
+    kb[q] = 0;
+    kv[q] = 0;
+    if (i < m) {
+      kb[q] = Ord::to_bits(io.src_keys[i]);
+      if constexpr (PAIRS) kv[q] = io.src_vals[i];
+      band &= kb[q];
+      bor |= kb[q];
+    }
+  }
+  __syncthreads();  // earlier readers of the shared memory are done
+  for (int i = tid; i < BL::kCntSlots; i += NT) CN[i] = 0u;
+  if (multi)
+    for (int i = tid; i < HW; i += NT) hb[i] = 0u;
+  {
+    const uint32_t a0 = __reduce_and_sync(0xFFFFFFFFu, static_cast<uint32_t>(band));
+    const uint32_t o0 = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(bor));
+    uint32_t a1 = 0, o1 = 0;
+    if constexpr (sizeof(Bits) == 8) {
+      a1 = __reduce_and_sync(0xFFFFFFFFu, static_cast<uint32_t>(static_cast<uint64_t>(band) >> 32));
+      o1 = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(static_cast<uint64_t>(bor) >> 32));
+    }
+    if (lane == 0) {
+      red_s[0][warp] = a0;
+      red_s[1][warp] = a1;
+      red_s[2][warp] = o0;
+      red_s[3][warp] = o1;
+    }
+  }
+  __syncthreads();
+  Bits all_and = ~Bits(0), all_or = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    Bits a = red_s[0][w], o = red_s[2][w];
+    if constexpr (sizeof(Bits) == 8) {
+      a |= static_cast<Bits>(red_s[1][w]) << 32;
+      o |= static_cast<Bits>(red_s[3][w]) << 32;
+    }
+    all_and &= a;
+    all_or |= o;
+  }
+  const Bits varying = all_and ^ all_or;  // bits that are not the same in every key
+  if (varying == 0) {
+    // Every key is equal: the stable order is the input order.
+    if (io.dst_keys != io.src_keys) {
+#pragma unroll
+      for (int q = 0; q < IPT; ++q) {
+        const int i = q * NT + tid;
+        if (i < m) {
+          io.dst_keys[i] = Ord::from_bits(kb[q]);
+          if constexpr (PAIRS) io.dst_vals[i] = kv[q];
+        }
+      }
+    }
+    __syncthreads();
+    return true;
+  }
+  const int sh = leading_zeros(varying);
+  // ---- segment heads; per head word the last head before it and the first
+  // after it ------------------------------------------------------------------------
+  if (multi) {
+    for (int64_t j = C.lo + tid; j < C.hi; j += NT) {
+      const int64_t p = off(j) - C.a;
+      if (p >= 0 && p < m) atomicOr(&hb[p >> 5], 1u << (p & 31));
+    }
+    __syncthreads();
+    if (warp == 0) {
+      int last[WPL], first[WPL];
+      int lmax = -1, lmin = m;
+#pragma unroll
+      for (int k = 0; k < WPL; ++k) {
+        const int w = lane * WPL + k;
+        const uint32_t x = hb[w];
+        last[k] = x ? (w << 5) + 31 - __clz(x) : -1;
+        first[k] = x ? (w << 5) + __ffs(x) - 1 : m;
+        lmax = max(lmax, last[k]);
+        lmin = min(lmin, first[k]);
+      }
+      // Exclusive running maximum over the lanes before, minimum over those after.
+      int pre = lmax, suf = lmin;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, pre, o);
+        const int z = __shfl_down_sync(0xFFFFFFFFu, suf, o);
+        if (lane >= o) pre = max(pre, y);
+        if (lane + o < 32) suf = min(suf, z);
+      }
+      pre = __shfl_up_sync(0xFFFFFFFFu, pre, 1);
+      suf = __shfl_down_sync(0xFFFFFFFFu, suf, 1);
+      if (lane == 0) pre = -1;
+      if (lane == 31) suf = m;
+#pragma unroll
+      for (int k = 0; k < WPL; ++k) {
+        hprev[lane * WPL + k] = pre;
+        pre = max(pre, last[k]);
+      }
+#pragma unroll
+      for (int k = WPL - 1; k >= 0; --k) {
+        hnext[lane * WPL + k] = suf;
+        suf = min(suf, first[k]);
+      }
+    }
+    __syncthreads();
+  }
+  // ---- bucket of every key; count (the old count is the key's slot) ----------------
+  uint32_t pk[IPT];
+#pragma unroll
+  for (int q = 0; q < IPT; ++q) {
+    const int i = q * NT + tid;
+    pk[q] = 0;
+    if (i < m) {
+      int s = 0, t = m;
+      if (multi) {
+        const int w = i >> 5, bit = i & 31;
+        const uint32_t x = hb[w];
+        const uint32_t below = x & (0xFFFFFFFFu >> (31 - bit));
+        s = below ? (w << 5) + 31 - __clz(below) : max(hprev[w], 0);
+        const uint32_t above = bit == 31 ? 0u : x & (0xFFFFFFFEu << bit);
+        t = above ? (w << 5) + __ffs(above) - 1 : hnext[w];
+      }
+      const uint32_t len = t > s ? static_cast<uint32_t>(t - s) : 1u;
+      int b = s + static_cast<int>(bucket_scale<Bits>(kb[q] << sh, len));
+      b = b < 0 ? 0 : (b >= m ? m - 1 : b);  // only malformed offsets reach the clamp
+      const uint32_t slot = atomicAdd(&CN[BL::cslot(b)], 1u);
+      pk[q] = static_cast<uint32_t>(b) | (slot << 16);
+    }
+  }
+  __syncthreads();
+  // ---- exclusive scan of the counts (thread t: buckets [t*IPT, t*IPT+IPT));
+  // sum of squared sizes and the largest bucket -------------------------------------
+  {
+    uint32_t sum = 0, sq = 0, mx = 0;
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      const uint32_t c = CN[BL::cslot(tid * IPT + j)];
+      sum += c;
+      sq += c * c;
+      mx = max(mx, c);
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_add<NT>(sum, total, warp_s);
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      uint32_t *at = CN + BL::cslot(tid * IPT + j);
+      const uint32_t c = *at;
+      *at = run;
+      run += c;
+    }
+    if (tid == 0) CN[BL::cslot(CAP)] = total;
+    const uint32_t sq_w = __reduce_add_sync(0xFFFFFFFFu, sq);
+    const uint32_t mx_w = __reduce_max_sync(0xFFFFFFFFu, mx);
+    if (lane == 0) {
+      red_s[0][warp] = sq_w;
+      red_s[1][warp] = mx_w;
+    }
+  }
+  __syncthreads();
+  uint32_t sq_all = 0, mx_all = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    sq_all += red_s[0][w];
+    mx_all = max(mx_all, red_s[1][w]);
+  }
+  if (sq_all > kBucketSkew * static_cast<uint32_t>(m) || mx_all > kBucketMaxSize) return false;
+  // ---- scatter to the buckets --------------------------------------------------------
+#pragma unroll
+  for (int q = 0; q < IPT; ++q) {
+    const int i = q * NT + tid;
+    if (i < m) {
+      const int b = static_cast<int>(pk[q] & 0xFFFFu);
+      const int p = static_cast<int>(CN[BL::cslot(b)] + (pk[q] >> 16));
+      SW[p] = WT::make(kb[q], static_cast<uint32_t>(i));
+      if constexpr (PAIRS) SV[p] = kv[q];
+      SB[p] = static_cast<uint16_t>(b);
+    }
+  }
+  __syncthreads();
+  // ---- every slot's key to its place: its bucket's start plus the bucket's
+  // words below it ----------------------------------------------------------------
+  for (int p = tid; p < m; p += NT) {
+    const int b = SB[p];
+    const int S = static_cast<int>(CN[BL::cslot(b)]);
+    const int E = static_cast<int>(CN[BL::cslot(b + 1)]);
+    const Word w = SW[p];
+    const int n = E - S;
+    int r = 0;
+    if (n > kBucketUnroll) {
+      for (int y = S; y < E; ++y) r += WT::lt(SW[y], w);
+    } else if (n > 1) {
+      // Fixed trip count: a warp whose buckets differ in size does not
+      // diverge.  Words past E (other buckets, or not written) are read but
+      // not counted; y stays inside the array.
+#pragma unroll
+      for (int k = 0; k < kBucketUnroll; ++k) {
+        const int y = min(S + k, CAP - 1);
+        r += (k < n) & WT::lt(SW[y], w);
+      }
+    }
+    io.dst_keys[S + r] = Ord::from_bits(WT::bits(w));
+    if constexpr (PAIRS) io.dst_vals[S + r] = SV[p];
+  }
+  __syncthreads();
+  return true;
+}
+
+}  // namespace segsort

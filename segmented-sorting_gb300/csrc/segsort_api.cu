@@ -64,7 +64,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   using Cfg = typename TileFor<K, PAIRS>::Cfg;
   auto tile_kernel = tile_sort_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
   static std::atomic<uint64_t> tile_attr_done{0};
-  if (ensure_smem(tile_kernel, Cfg::kSmemBytes, tile_attr_done, dev) != cudaSuccess)
+  if (ensure_smem(tile_kernel, tile_smem_bytes<Cfg, PAIRS>(), tile_attr_done, dev) != cudaSuccess)
     return SEGSORT_ERR_CUDA;
   const int64_t tiles = (n + Cfg::CAP - 1) / Cfg::CAP;
   const bool prof = g_prof_on.load(std::memory_order_relaxed);
@@ -73,7 +73,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // ---- one tile: every segment fits, no workspace, one kernel ---------------
   if (tiles == 1) {
     if (prof) rec.t0 = prof_event(stream);
-    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr, nullptr, nullptr,
+    tile_kernel<<<1, Cfg::NT, tile_smem_bytes<Cfg, PAIRS>(), stream>>>(keys, vals, off, nullptr, nullptr, nullptr,
                                                           0);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     if (prof) {
@@ -153,7 +153,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
                                                            W.tmp_keys, W.tmp_vals, tiles,
                                                            W.radix_min);
     } else {
-      tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
+      tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, tile_smem_bytes<Cfg, PAIRS>(), stream>>>(
           keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
     }
     if (prof) rec.t1 = prof_event(stream);

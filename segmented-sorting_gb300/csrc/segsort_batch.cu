@@ -156,7 +156,7 @@ struct BatchKernels {
 
   // Attributes and occupancy, before any capture.
   static cudaError_t prepare(int dev) {
-    cudaError_t e = ensure_smem(tile, TCfg::kSmemBytes, tile_attr, dev);
+    cudaError_t e = ensure_smem(tile, tile_smem_bytes<TCfg, true>(), tile_attr, dev);
     if (e == cudaSuccess) e = ensure_smem(merge, MS::kBytes, merge_attr, dev);
     if (e == cudaSuccess) occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     return e;
@@ -178,7 +178,7 @@ struct BatchKernels {
 
     // Tile sort first: it forms the sorted runs the merge passes read (the
     // radix passes read the caller's buffers, which it leaves alone).
-    tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, TCfg::kSmemBytes, stream>>>(
+    tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, tile_smem_bytes<TCfg, true>(), stream>>>(
         tab, count, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
