@@ -381,12 +381,17 @@ int segsort_pool_bytes(int *created, uint64_t *used);
  *     segments by merge passes over tile-sorted runs.  At least 4096.
  *   SEGSORT_PARAM_STREAM_MAX_AVG: problems whose average segment (n / nseg)
  *     is at most this long take the streamed short-segment tile kernel.
+ *   SEGSORT_PARAM_BUCKET_MIN_AVG: other problems whose average segment is at
+ *     least this long take the bucket route of the tile sort (a bucket sort
+ *     by key value per chunk, the comparison sort for the chunks it
+ *     refuses); 0 turns the route off.
  * A change applies to calls made after it; batch plans keep the values they
  * were created with.  SEGSORT_ERR_INVALID_ARG for an unknown parameter or a
  * value out of range. */
 #define SEGSORT_PARAM_RADIX_MIN_32 1
 #define SEGSORT_PARAM_RADIX_MIN_64 2
 #define SEGSORT_PARAM_STREAM_MAX_AVG 3
+#define SEGSORT_PARAM_BUCKET_MIN_AVG 4
 int segsort_set_param(int param, int64_t value);
 int segsort_get_param(int param, int64_t *value);
 

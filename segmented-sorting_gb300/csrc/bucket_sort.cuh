@@ -90,10 +90,10 @@ constexpr size_t tile_smem_bytes() {
 // ends with a barrier, so it may follow and precede any other use of the
 // shared memory.
 template <typename Cfg, bool PAIRS, typename K>
-__device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint32_t *vals,
-                                               const Offsets &off, K *tmp_keys,
-                                               uint32_t *tmp_vals, unsigned char *smem,
-                                               uint32_t *hb, int *warp_s) {
+__device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, uint32_t *vals,
+                                                 const Offsets &off, K *tmp_keys,
+                                                 uint32_t *tmp_vals, unsigned char *smem,
+                                                 uint32_t *hb, int *warp_s) {
   using Ord = typename Cfg::Ord;
   using Bits = typename Cfg::Bits;
   using WT = typename Cfg::WT;
@@ -329,6 +329,69 @@ __device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint
   }
   __syncthreads();
   return true;
+}
+
+// The same, not inlined, for the comparison-sort kernels that try it first
+// (the batched tile kernel).
+template <typename Cfg, bool PAIRS, typename K>
+__device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint32_t *vals,
+                                               const Offsets &off, K *tmp_keys,
+                                               uint32_t *tmp_vals, unsigned char *smem,
+                                               uint32_t *hb, int *warp_s) {
+  return bucket_sort_body<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s);
+}
+
+// ---------------------------------------------------------------------------
+// The bucket route of the tile sort: two kernels.  tile_bucket_kernel: CTA t
+// plans tile t (plan_tile) and bucket-sorts its chunks; a chunk of segments
+// shorter than kBucketMinAvg on average, or one the bucket sort refuses, is
+// appended to the fallback list.  tile_list_kernel: persistent CTAs sort the
+// listed chunks with the comparison sort (its own launch shape: 256 threads,
+// 128 registers).  The list holds at most kMaxTileChunks chunks per tile.
+// ---------------------------------------------------------------------------
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_bucket_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
+                   const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
+                   uint32_t *__restrict__ tmp_vals, int64_t radix_min, TileChunk *fallback,
+                   uint32_t *fallback_count, int64_t max_fallback) {
+  using Cfg = TileConfig<K, PAIRS, NT, KPT>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ TilePlan plan_s;
+  __shared__ uint32_t hb[Cfg::CAP / 32];
+  __shared__ int warp_s[NT / 16];
+  const int64_t t = blockIdx.x;
+  if (t * Cfg::CAP >= off.n) return;
+  if (threadIdx.x == 0)
+    plan_tile<Cfg::CAP>(off, half_first, t, tmp_keys != nullptr, radix_min, plan_s);
+  __syncthreads();
+  const int nc = plan_s.nc;
+  for (int c = 0; c < nc; ++c) {
+    const TileChunk &C = plan_s.c[c];
+    if (static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg <= C.m &&
+        bucket_sort_body<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s))
+      continue;
+    if (threadIdx.x == 0) {
+      const uint32_t at = atomicAdd(fallback_count, 1u);
+      if (at < max_fallback) fallback[at] = C;
+    }
+  }
+}
+
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_list_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
+                 K *__restrict__ tmp_keys, uint32_t *__restrict__ tmp_vals,
+                 const TileChunk *__restrict__ list, const uint32_t *count, int64_t max_list) {
+  using Cfg = TileConfig<K, PAIRS, NT, KPT>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t hb[Cfg::CAP / 32];
+  __shared__ int warp_s[NT / 16];
+  const int64_t c = min(static_cast<int64_t>(*count), max_list);
+  for (int64_t i = blockIdx.x; i < c; i += gridDim.x) {
+    const TileChunk C = list[i];
+    sort_tile_chunk<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s);
+  }
 }
 
 }  // namespace segsort

@@ -28,8 +28,11 @@ enum : int {
   kCtrRJobs = 8,      // segments for the radix passes found by classify
   kCtrRTiles = 9,     // radix tiles of all radix jobs
   kCtrRDigits = 10,   // OR over radix jobs of their digits that vary
+  kCtrFallback = 11,  // tile chunks the bucket sort left to the comparison sort
   kCtrWords = 16,
 };
+
+struct TileChunk;  // tile_sort.cuh
 
 // Device views of the workspace.
 template <typename K>
@@ -49,6 +52,8 @@ struct LargeWs {
   uint32_t *rdigits;      // [max_rjobs] digits of the job's keys that vary (bit d: digit d)
   uint32_t *rhist;        // [max_rjobs][digits][256] digit counts, then bucket starts
   unsigned long long *rlook;  // [max_rtiles][256] look-back words of the radix tiles
+  TileChunk *fallback;    // [max_fallback] chunks for the comparison sort (bucket route)
+  int64_t max_fallback;
   int32_t max_jobs;
   int32_t max_rjobs;
   int64_t max_items;

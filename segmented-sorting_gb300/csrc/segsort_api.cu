@@ -64,7 +64,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   using Cfg = typename TileFor<K, PAIRS>::Cfg;
   auto tile_kernel = tile_sort_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
   static std::atomic<uint64_t> tile_attr_done{0};
-  if (ensure_smem(tile_kernel, tile_smem_bytes<Cfg, PAIRS>(), tile_attr_done, dev) != cudaSuccess)
+  if (ensure_smem(tile_kernel, Cfg::kSmemBytes, tile_attr_done, dev) != cudaSuccess)
     return SEGSORT_ERR_CUDA;
   const int64_t tiles = (n + Cfg::CAP - 1) / Cfg::CAP;
   const bool prof = g_prof_on.load(std::memory_order_relaxed);
@@ -73,7 +73,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // ---- one tile: every segment fits, no workspace, one kernel ---------------
   if (tiles == 1) {
     if (prof) rec.t0 = prof_event(stream);
-    tile_kernel<<<1, Cfg::NT, tile_smem_bytes<Cfg, PAIRS>(), stream>>>(keys, vals, off, nullptr, nullptr, nullptr,
+    tile_kernel<<<1, Cfg::NT, Cfg::kSmemBytes, stream>>>(keys, vals, off, nullptr, nullptr, nullptr,
                                                           0);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     if (prof) {
@@ -119,6 +119,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // of dependent loads).  The two write the same map and jobs.
     const bool short_avg =
         R.stream_max_avg > 0 && n <= R.stream_max_avg * static_cast<int64_t>(nseg);
+    const int64_t bucket_min = g_bucket_min_avg.load(std::memory_order_relaxed);
     if (short_avg) {
       const unsigned blocks =
           static_cast<unsigned>((W.halves + kClassifyWarps) / kClassifyWarps);  // halves + 1 entries
@@ -152,8 +153,33 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       stream_kernel<<<grid, Cfg::NT, SL::kBytes, stream>>>(keys, vals, off, W.half_first,
                                                            W.tmp_keys, W.tmp_vals, tiles,
                                                            W.radix_min);
+    } else if (bucket_min > 0 && n >= bucket_min * static_cast<int64_t>(nseg)) {
+      // Bucket route: the bucket kernel sorts the chunks it can and lists the
+      // others; persistent comparison-sort CTAs take the list.
+      using BF = BucketFor<K, PAIRS>;
+      using BCfg = typename BF::Cfg;
+      constexpr size_t kBSmem = BucketLayout<BCfg, PAIRS>::kBytes;
+      auto bucket_kernel = tile_bucket_kernel<K, PAIRS, BCfg::NT, BCfg::KPT, BF::kMinBlocks>;
+      auto list_kernel =
+          tile_list_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
+      static std::atomic<uint64_t> bucket_attr_done{0}, list_attr_done{0};
+      static std::atomic<int> list_occ[kMaxDevices];
+      if (ensure_smem(bucket_kernel, kBSmem, bucket_attr_done, dev) != cudaSuccess ||
+          ensure_smem(list_kernel, Cfg::kSmemBytes, list_attr_done, dev) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      bucket_kernel<<<static_cast<unsigned>(tiles), BCfg::NT, kBSmem, stream>>>(
+          keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min, W.fallback,
+          W.ctr + kCtrFallback, W.max_fallback);
+      const int lo = occupancy(list_kernel, Cfg::NT, Cfg::kSmemBytes, list_occ, dev);
+      const unsigned lgrid =
+          static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, tiles));
+      list_kernel<<<lgrid, Cfg::NT, Cfg::kSmemBytes, stream>>>(
+          keys, vals, off, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
+          W.max_fallback);
     } else {
-      tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, tile_smem_bytes<Cfg, PAIRS>(), stream>>>(
+      tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
           keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
     }
     if (prof) rec.t1 = prof_event(stream);
@@ -508,6 +534,10 @@ int segsort_set_param(int param, int64_t value) {
       if (value < 0) return SEGSORT_ERR_INVALID_ARG;
       g_stream_max_avg.store(value, std::memory_order_relaxed);
       return SEGSORT_OK;
+    case SEGSORT_PARAM_BUCKET_MIN_AVG:
+      if (value < 0) return SEGSORT_ERR_INVALID_ARG;
+      g_bucket_min_avg.store(value, std::memory_order_relaxed);
+      return SEGSORT_OK;
     default:
       return SEGSORT_ERR_INVALID_ARG;
   }
@@ -521,6 +551,9 @@ int segsort_get_param(int param, int64_t *value) {
     case SEGSORT_PARAM_RADIX_MIN_64: *value = radix_min_for<uint64_t>(); return SEGSORT_OK;
     case SEGSORT_PARAM_STREAM_MAX_AVG:
       *value = g_stream_max_avg.load(std::memory_order_relaxed);
+      return SEGSORT_OK;
+    case SEGSORT_PARAM_BUCKET_MIN_AVG:
+      *value = g_bucket_min_avg.load(std::memory_order_relaxed);
       return SEGSORT_OK;
     default:
       return SEGSORT_ERR_INVALID_ARG;

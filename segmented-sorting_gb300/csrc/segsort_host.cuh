@@ -45,6 +45,17 @@ struct TileFor {
   static constexpr int kMinBlocks = SEGSORT_TILE_MINB;  // resident CTAs per SM the registers must allow
 };
 
+// Launch shape of the bucket-route tile kernel (tile_bucket_kernel): the
+// same tile capacity, 512 threads.  At 64 registers two CTAs fill an SM with
+// 32 warps; measured on GB300 (2^24 u32 pairs, 2^12-key segments) 0.16 ms
+// against 0.19 ms for 256 threads at 128 registers.
+template <typename K, bool PAIRS>
+struct BucketFor {
+  static constexpr int kNT = 512;
+  using Cfg = TileConfig<K, PAIRS, kNT, TileFor<K, PAIRS>::Cfg::CAP / kNT>;
+  static constexpr int kMinBlocks = 2;
+};
+
 template <typename K>
 constexpr int64_t tile_cap() {
   return TileFor<K, false>::Cfg::CAP;
@@ -81,6 +92,13 @@ inline int64_t radix_min_for() {
 // (segsort_set_param); a huge value sends every multi-tile problem through
 // them.
 inline std::atomic<int64_t> g_stream_max_avg{32};
+
+// Problems (not streamed) whose average segment is at least this long take
+// the bucket route of the tile sort (tile_bucket_kernel, then
+// tile_list_kernel for the chunks it refuses); 0: never.  Below 128 keys per
+// segment the comparison sort is faster (measured on GB300, 2^24 u32 pairs:
+// 0.20 against 0.25 ms at 64, even at 128).  Run-time parameter.
+inline std::atomic<int64_t> g_bucket_min_avg{128};
 
 // ---------------------------------------------------------------------------
 // Route of one plain call: the radix threshold, the streamed-tile threshold
@@ -139,8 +157,9 @@ inline CallRoute route_for(int64_t n, int32_t nseg) {
 struct WsLayout {
   size_t ctr = 0, jobs = 0, prefix = 0, half_first = 0, item_job = 0, split = 0, item_desc = 0,
          tmp_keys = 0, tmp_vals = 0, rjobs = 0, rprefix = 0, rtile_desc = 0, rdigits = 0,
-         rhist = 0, rlook = 0;
+         rhist = 0, rlook = 0, fallback = 0;
   size_t total = 0;
+  int64_t max_fallback = 0;
   int32_t max_jobs = 0;
   int32_t max_rjobs = 0;
   int64_t max_items = 0;
@@ -195,6 +214,9 @@ constexpr WsLayout make_layout(int64_t n, int key_bytes, int val_bytes, int64_t 
   L.rdigits = take(mr * 4);
   L.rhist = take(mr * digits * kRBuckets * 4);
   L.rlook = take(static_cast<size_t>(L.max_rtiles) * kRBuckets * 8);
+  // Every chunk of every tile may fall back from the bucket sort.
+  L.max_fallback = kMaxTileChunks * ((L.halves + 1) / 2 + 1);
+  L.fallback = take(static_cast<size_t>(L.max_fallback) * sizeof(TileChunk));
   L.tmp_keys = take(static_cast<size_t>(n) * key_bytes);
   L.tmp_vals = take(static_cast<size_t>(n) * val_bytes);
   L.total = off;
@@ -233,6 +255,8 @@ inline LargeWs<K> ws_views(unsigned char *base, const WsLayout &L) {
   W.rdigits = reinterpret_cast<uint32_t *>(base + L.rdigits);
   W.rhist = reinterpret_cast<uint32_t *>(base + L.rhist);
   W.rlook = reinterpret_cast<unsigned long long *>(base + L.rlook);
+  W.fallback = reinterpret_cast<TileChunk *>(base + L.fallback);
+  W.max_fallback = L.max_fallback;
   W.max_jobs = L.max_jobs;
   W.max_rjobs = L.max_rjobs;
   W.max_items = L.max_items;

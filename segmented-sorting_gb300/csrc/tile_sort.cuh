@@ -844,17 +844,14 @@ __device__ __forceinline__ void sort_tile_chunk(const TileChunk &C, K *keys, uin
 
 // Bucket sort of a chunk (bucket_sort.cuh): false when the chunk's keys are
 // too skewed for it, having written nothing.  Not inlined: the comparison
-// sort below keeps its own register allocation (inlined together, the two
-// spill).
+// sort of a kernel that tries it first keeps its own register allocation
+// (inlined together, the two spill).
 template <typename Cfg, bool PAIRS, typename K>
 __device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint32_t *vals,
                                                const Offsets &off, K *tmp_keys,
                                                uint32_t *tmp_vals, unsigned char *smem,
                                                uint32_t *hb, int *warp_s);
 
-#ifndef SEGSORT_TILE_BUCKET
-#define SEGSORT_TILE_BUCKET 1
-#endif
 // Shortest average segment of a chunk the bucket sort is tried on: below it
 // the comparison sort is faster (its merge levels stop at the segment length;
 // on GB300, 2^24 u32 pairs: 0.20 against 0.25 ms at 64 keys per segment, even
@@ -865,9 +862,10 @@ constexpr int64_t kBucketMinAvg = 128;
 // One CTA of the tile sort: tile t of a problem whose half-tile map is
 // half_first (null: the problem is one tile).  With tmp_keys given the CTA
 // also forms the CAP-runs of the long segments of at most radix_min
-// elements (plan_tile).
+// elements (plan_tile).  kBucket: chunks of segments of kBucketMinAvg keys
+// or more on average try the bucket sort first.
 // ---------------------------------------------------------------------------
-template <typename K, bool PAIRS, int NT, int KPT>
+template <typename K, bool PAIRS, int NT, int KPT, bool kBucket = false>
 __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restrict__ vals,
                                          const Offsets &off, const int32_t *__restrict__ half_first,
                                          int64_t t, K *__restrict__ tmp_keys = nullptr,
@@ -886,7 +884,7 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
   const int nc = plan_s.nc;
   for (int c = 0; c < nc; ++c) {
     const TileChunk &C = plan_s.c[c];
-    if (SEGSORT_TILE_BUCKET && static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg <= C.m &&
+    if (kBucket && static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg <= C.m &&
         bucket_sort_chunk<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s))
       continue;
     sort_tile_chunk<Cfg, PAIRS>(plan_s.c[c], keys, vals, off, tmp_keys, tmp_vals, smem, hb,
@@ -920,7 +918,7 @@ tile_sort_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
   const int64_t t = blockIdx.x;
   const int32_t i = find_instance(tab, count, t, &BatchInst::tile_base);
   const BatchInst &I = tab[i];
-  tile_cta<K, PAIRS, NT, KPT>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
+  tile_cta<K, PAIRS, NT, KPT, true>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
                               half_first + I.half_base, t - I.tile_base, tmp_keys + I.tmp_base,
                               PAIRS ? tmp_vals + I.tmp_base : nullptr, radix_min);
 }
