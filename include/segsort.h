@@ -385,6 +385,11 @@ int segsort_pool_bytes(int *created, uint64_t *used);
  *     least this long take the bucket route of the tile sort (a bucket sort
  *     by key value per chunk, the comparison sort for the chunks it
  *     refuses); 0 turns the route off.
+ *   SEGSORT_PARAM_MSD: 1 (default) or 0.  With 1, a call whose average
+ *     segment is longer than the radix threshold, in the library's own
+ *     workspace, sorts its radix segments whose keys vary in at least three
+ *     8-bit digits by one radix pass on the top varying digit and then the
+ *     tile sort of the 256 sub-buckets, instead of one pass per digit.
  * A change applies to calls made after it; batch plans keep the values they
  * were created with.  SEGSORT_ERR_INVALID_ARG for an unknown parameter or a
  * value out of range. */
@@ -392,6 +397,7 @@ int segsort_pool_bytes(int *created, uint64_t *used);
 #define SEGSORT_PARAM_RADIX_MIN_64 2
 #define SEGSORT_PARAM_STREAM_MAX_AVG 3
 #define SEGSORT_PARAM_BUCKET_MIN_AVG 4
+#define SEGSORT_PARAM_MSD 5
 int segsort_set_param(int param, int64_t value);
 int segsort_get_param(int param, int64_t *value);
 

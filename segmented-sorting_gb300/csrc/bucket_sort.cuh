@@ -184,12 +184,23 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     return true;
   }
   const int sh = leading_zeros(varying);
+  // Order bits the keys of a segment share, when the offsets say (the MSD
+  // route's sub-buckets): shifted out too, so that the segment's keys spread
+  // over its buckets.  Per head position in SH (over the bucket indices'
+  // region, unused until the scatter).
+  uint8_t *SH = reinterpret_cast<uint8_t *>(smem + BL::kBkt);
+  const bool hinted = off.flags != nullptr;
+  const int seg_sh = hinted && !multi ? (off.flags[C.lo] & kSegShared) : 0;
   // ---- segment heads; per head word the last head before it and the first
   // after it ------------------------------------------------------------------------
   if (multi) {
     for (int64_t j = C.lo + tid; j < C.hi; j += NT) {
-      const int64_t p = off(j) - C.a;
-      if (p >= 0 && p < m) atomicOr(&hb[p >> 5], 1u << (p & 31));
+      const int64_t b0 = off(j);
+      const int64_t p = b0 - C.a;
+      if (p >= 0 && p < m) {
+        atomicOr(&hb[p >> 5], 1u << (p & 31));
+        if (hinted && off(j + 1) > b0) SH[p] = off.flags[j] & kSegShared;
+      }
     }
     __syncthreads();
     if (warp == 0) {
@@ -247,7 +258,10 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
         t = above ? (w << 5) + __ffs(above) - 1 : hnext[w];
       }
       const uint32_t len = t > s ? static_cast<uint32_t>(t - s) : 1u;
-      int b = s + static_cast<int>(bucket_scale<Bits>(kb[q] << sh, len));
+      int shift = sh;
+      if (hinted) shift = max(shift, multi ? static_cast<int>(SH[s]) : seg_sh);
+      shift = min(shift, static_cast<int>(8 * sizeof(Bits)) - 1);
+      int b = s + static_cast<int>(bucket_scale<Bits>(kb[q] << shift, len));
       b = b < 0 ? 0 : (b >= m ? m - 1 : b);  // only malformed offsets reach the clamp
       const uint32_t slot = atomicAdd(&CN[BL::cslot(b)], 1u);
       pk[q] = static_cast<uint32_t>(b) | (slot << 16);

@@ -38,7 +38,7 @@ struct TileChunk;  // tile_sort.cuh
 template <typename K>
 struct LargeWs {
   uint32_t *ctr;          // [kCtrWords]
-  int4 *jobs;             // [max_jobs] merge segments: {begin, end, 0, instance}
+  int4 *jobs;             // [max_jobs] merge segments: {begin, end, segment or 0, instance}
   int32_t *item_prefix;   // [max_jobs + 1] merge items before each job
   int32_t *half_first;    // [halves + 1] first segment starting at or after h * CAP/2
   int32_t *item_job;      // [max_items] job of each merge item
@@ -46,7 +46,7 @@ struct LargeWs {
   int4 *item_desc;        // [2 * max_items] item descriptors of the current pass
   K *tmp_keys;            // [n]
   uint32_t *tmp_vals;     // [n]
-  int4 *rjobs;            // [max_rjobs] radix segments: {begin, end, 0, instance}
+  int4 *rjobs;            // [max_rjobs] radix segments: {begin, end, segment or 0, instance}
   int32_t *rtile_prefix;  // [max_rjobs + 1] radix tiles before each radix job
   int4 *rtile_desc;       // [max_rtiles] radix tiles: {first position, length, job, index in job}
   uint32_t *rdigits;      // [max_rjobs] digits of the job's keys that vary (bit d: digit d)
@@ -60,6 +60,11 @@ struct LargeWs {
   int64_t halves;
   int64_t max_rtiles;
   int64_t radix_min;      // segments longer than this take the radix passes
+  // 1: first stage of the MSD route (radix_sort.cuh): the radix segments that
+  // qualify run one pass on their top varying digit, the others all their
+  // passes; the long-segment kernel then returns before the merge passes.
+  int32_t msd_stage;
+  int32_t tile_cap;       // keys per tile of the tile sort
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -94,10 +99,12 @@ __device__ __forceinline__ void classify_boundary(const Offsets &off, int64_t s,
     const int64_t h_hi = s == off.nseg ? halves : min(cur / half, halves);
     for (int64_t h = h_lo; h <= h_hi; ++h) half_first[h] = static_cast<int32_t>(s);
     if (s < off.nseg) len = off(s + 1) - cur;
+    if (off.flags != nullptr && s < off.nseg && (off.flags[s] & kSegSkip)) len = 0;  // sorted
   }
   const bool rlarge = len > ws.radix_min;
   const bool large = len > cap && !rlarge;
-  const int4 job = make_int4(static_cast<int32_t>(cur), static_cast<int32_t>(cur + len), 0, inst);
+  const int4 job = make_int4(static_cast<int32_t>(cur), static_cast<int32_t>(cur + len),
+                            static_cast<int32_t>(s), inst);
   const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, large);
   if (ballot != 0) {
     uint32_t base = 0;

@@ -207,6 +207,7 @@ long_segment_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
   __shared__ int maxp_s;
 
   radix_phases<K, PAIRS, NT>(sp, ws, smem, warp_s);
+  if (ws.msd_stage) return;  // the merge passes run after the tile sort of the sub-buckets
 
   const int tid = threadIdx.x;
   const int64_t G = gridDim.x;

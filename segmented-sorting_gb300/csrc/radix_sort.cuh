@@ -68,6 +68,18 @@ constexpr int kRItems = 16;             // keys per thread in a radix tile
 constexpr int kLookSpinLimit = 1 << 22;  // ~0.3 s with the back-off below
 constexpr int kLookWindow = 16;          // predecessors read per look-back round
 constexpr int kLookEagerSpins = 32;      // polls before the look-back backs off
+// rdigits flag of a segment on the MSD route: its digit mask holds only its
+// top varying digit (one pass); the pass count and buffer parity use the
+// mask bits alone.
+constexpr uint32_t kRDigitMsd = 1u << 16;
+constexpr uint32_t kRDigitMask = kRDigitMsd - 1u;
+// A segment takes the MSD route when at least this many digit positions vary
+// (fewer LSD passes cost less than the MSD pass, its copy-back and the tile
+// pass over the sub-buckets) ...
+constexpr int kMsdMinDigits = 3;
+// ... and no bucket of its top varying digit holds more than this many keys
+// times the tile capacity (a larger sub-bucket takes the merge passes).
+constexpr int kMsdMaxBucketTiles = 2;
 
 template <typename K, bool PAIRS, int NT>
 struct RadixShape {
@@ -424,6 +436,23 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       gh[d * kRBuckets + tid] = block_exclusive_add<NT>(c[d], tot, warp_s);
       if (!__syncthreads_or(c[d] == len)) varying |= 1u << d;
     }
+    if (ws.msd_stage && __popc(varying) >= kMsdMinDigits) {
+      // MSD route when the top varying digit splits the segment into
+      // sub-buckets the tile sort can take.
+      const int dt = 31 - __clz(varying);
+      uint32_t mine = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) mine = d == dt ? c[d] : mine;
+      const uint32_t wmax = __reduce_max_sync(0xFFFFFFFFu, mine);
+      if (lane == 0) warp_s[warp] = static_cast<int>(wmax);
+      __syncthreads();
+      uint32_t mx = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) mx = max(mx, static_cast<uint32_t>(warp_s[w]));
+      __syncthreads();
+      if (mx <= static_cast<uint32_t>(kMsdMaxBucketTiles * ws.tile_cap))
+        varying = (1u << dt) | kRDigitMsd;
+    }
     if (tid == 0) {
       ws.rdigits[j] = varying;
       if (varying) atomicOr(&ws.ctr[kCtrRDigits], varying);
@@ -630,7 +659,7 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
   // ---- segments that ran an odd number of passes: tmp -> caller ------------
   for (int64_t t = blockIdx.x; t < ntiles; t += G) {
     const int4 de = ws.rtile_desc[t];
-    if (!(__popc(ws.rdigits[de.z]) & 1)) continue;
+    if (!(__popc(ws.rdigits[de.z] & kRDigitMask) & 1)) continue;
     const int cnt = de.y;
     const SideBuffers<K> B = sp(ws.rjobs[de.z].w);
     K kk[IPT];

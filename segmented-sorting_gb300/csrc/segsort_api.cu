@@ -20,6 +20,8 @@ namespace {
 // Opt-in phase timing (segsort_profile_enable / segsort_profile_read).
 struct PhaseRecord {
   cudaEvent_t t0 = nullptr, t1 = nullptr, l0 = nullptr, l1 = nullptr;
+  cudaEvent_t m0 = nullptr, m1 = nullptr;  // stage 1 of the MSD route (counted as large)
+  int tile_launches = 1;
   int large_launches = 0;
 };
 std::atomic<bool> g_prof_on{false};
@@ -89,12 +91,31 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // (segsort_workspace_bytes); the library's own is sized for the current one.
   const WsLayout L =
       ws != nullptr ? layout_any_threshold<K, PAIRS>(n) : layout_for<K, PAIRS>(n, R.radix_min);
+  // MSD route (msd_route.cuh): problems whose average segment is longer than
+  // the radix threshold, in a workspace the library owns (the expansion's
+  // arrays grow with nseg).
+  const bool msd = g_msd_on.load(std::memory_order_relaxed) != 0 && ws == nullptr &&
+                   n > std::max<int64_t>(L.radix_min, R.radix_min) * static_cast<int64_t>(nseg);
+  const int64_t c_len = msd ? msd_stage2_segments(nseg, L.max_rjobs) : 0;
+  size_t msd_at[6] = {0, 0, 0, 0, 0, 0};  // sub, flags, jbeg, jidx, jextra, end
+  if (msd) {
+    const size_t rj = static_cast<size_t>(L.max_rjobs) + 1;
+    const size_t sizes[5] = {static_cast<size_t>(c_len + 1) * 4, static_cast<size_t>(c_len),
+                             rj * 4, rj * 4, rj * 4};
+    size_t at = L.total;
+    for (int i = 0; i < 5; ++i) {
+      msd_at[i] = at;
+      at = align256(at + sizes[i]);
+    }
+    msd_at[5] = at;
+  }
+  const size_t alloc_bytes = msd ? msd_at[5] : L.total;
   bool owned = false;
   unsigned char *base = static_cast<unsigned char *>(ws);
   if (base == nullptr) {
     cudaMemPool_t pool = device_pool(*S, dev);
     if (pool == nullptr ||
-        cudaMallocFromPoolAsync(reinterpret_cast<void **>(&base), L.total, pool, stream) !=
+        cudaMallocFromPoolAsync(reinterpret_cast<void **>(&base), alloc_bytes, pool, stream) !=
             cudaSuccess) {
       cudaGetLastError();
       return SEGSORT_ERR_NO_MEMORY;
@@ -107,8 +128,66 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   LargeWs<K> W = ws_views<K, PAIRS>(base, L);
   W.radix_min = std::max<int64_t>(L.radix_min, R.radix_min);
 
+  // The long-segment kernel: radix passes, then merge passes, one cooperative
+  // launch (returns at once without long segments).  All resident CTAs, but
+  // no more than one per merge item of the whole problem: small calls then
+  // leave the rest of the GPU to other work.
+  using MS = LongSmem<K, PAIRS>;
+  auto merge_kernel = long_segment_kernel<K, PAIRS, SingleSpace<K>>;
+  static std::atomic<uint64_t> merge_attr_done{0};
+  static std::atomic<int> merge_occ[kMaxDevices];
+  auto launch_long = [&](LargeWs<K> &Wl) -> int {
+    if (!S->coop || ensure_smem(merge_kernel, MS::kBytes, merge_attr_done, dev) != cudaSuccess)
+      return SEGSORT_ERR_CUDA;
+    const int mo = occupancy(merge_kernel, kMThreads, MS::kBytes, merge_occ, dev);
+    const int per_sm = R.merge_per_sm > 0 ? std::min(R.merge_per_sm, mo) : mo;
+    const int64_t items = n / MergeShape<K>::T + 1;
+    const unsigned merge_grid =
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(per_sm) * S->sms, items));
+    SingleSpace<K> sp{keys, vals, W.tmp_keys, W.tmp_vals};
+    int64_t cap = tile_cap<K>();
+    void *args[] = {&sp, &Wl, &cap};
+    if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(merge_kernel), dim3(merge_grid),
+                                    dim3(kMThreads), args, MS::kBytes, stream) != cudaSuccess)
+      return SEGSORT_ERR_CUDA;
+    return SEGSORT_OK;
+  };
+  auto segment_classify = [&](const Offsets &o) {
+    const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(o.nseg) + 1 + 255) / 256);
+    large_classify_kernel<K><<<blocks, 256, 0, stream>>>(o, tile_cap<K>(), tile_cap<K>() / 2, W);
+  };
+
   int rc = SEGSORT_OK;
   do {
+    Offsets O = off;  // the offsets the tile sort and the merge passes see
+    if (msd) {
+      // ---- MSD route, stage 1 and the expansion (msd_route.cuh) ------------
+      MsdWs M{reinterpret_cast<int32_t *>(base + msd_at[0]),
+              reinterpret_cast<uint8_t *>(base + msd_at[1]), c_len,
+              reinterpret_cast<int32_t *>(base + msd_at[2]),
+              reinterpret_cast<int32_t *>(base + msd_at[3]),
+              reinterpret_cast<int32_t *>(base + msd_at[4])};
+      if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      segment_classify(off);
+      if (prof) rec.m0 = prof_event(stream);
+      W.msd_stage = 1;
+      rc = launch_long(W);
+      W.msd_stage = 0;
+      if (rc != SEGSORT_OK) break;
+      msd_rank_kernel<K><<<static_cast<unsigned>((W.max_rjobs + 255) / 256), 256, 0, stream>>>(W, M);
+      msd_expand_kernel<K><<<static_cast<unsigned>((static_cast<int64_t>(nseg) + 256) / 256), 256,
+                             0, stream>>>(off, W, M);
+      msd_sub_kernel<K><<<static_cast<unsigned>(W.max_rjobs), kRBuckets, 0, stream>>>(W, M);
+      if (prof) rec.m1 = prof_event(stream);
+      if (cudaGetLastError() != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      O = Offsets{M.sub, static_cast<int32_t>(c_len), 0, n, M.flags};
+    }
     // ---- classify: half-tile -> first segment map, jobs for long segments ----
     if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess) {
       rc = SEGSORT_ERR_CUDA;
@@ -116,9 +195,11 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     }
     // Short segments on average: one search per half-tile (work ~ n / CAP);
     // otherwise one thread per segment boundary (work ~ nseg, fewer rounds
-    // of dependent loads).  The two write the same map and jobs.
+    // of dependent loads).  The two write the same map and jobs.  The MSD
+    // route's sub-buckets are long on average (the expansion pads the
+    // offsets with empty segments, so n / O.nseg understates them).
     const bool short_avg =
-        R.stream_max_avg > 0 && n <= R.stream_max_avg * static_cast<int64_t>(nseg);
+        !msd && R.stream_max_avg > 0 && n <= R.stream_max_avg * static_cast<int64_t>(nseg);
     const int64_t bucket_min = g_bucket_min_avg.load(std::memory_order_relaxed);
     if (short_avg) {
       const unsigned blocks =
@@ -126,8 +207,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       large_classify_halves_kernel<K><<<blocks, (kClassifyWarps + 1) * 32, 0, stream>>>(
           off, tile_cap<K>(), tile_cap<K>() / 2, W);
     } else {
-      const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(nseg) + 1 + 255) / 256);
-      large_classify_kernel<K><<<blocks, 256, 0, stream>>>(off, tile_cap<K>(), tile_cap<K>() / 2, W);
+      segment_classify(O);
     }
 
     // ---- tile sort: every segment of at most CAP elements, and the sorted
@@ -150,10 +230,10 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       const int so = occupancy(stream_kernel, Cfg::NT, SL::kBytes, stream_occ, dev);
       const unsigned grid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(so) * S->sms, tiles));
-      stream_kernel<<<grid, Cfg::NT, SL::kBytes, stream>>>(keys, vals, off, W.half_first,
+      stream_kernel<<<grid, Cfg::NT, SL::kBytes, stream>>>(keys, vals, O, W.half_first,
                                                            W.tmp_keys, W.tmp_vals, tiles,
                                                            W.radix_min);
-    } else if (bucket_min > 0 && n >= bucket_min * static_cast<int64_t>(nseg)) {
+    } else if (bucket_min > 0 && (msd || n >= bucket_min * static_cast<int64_t>(nseg))) {
       // Bucket route: the bucket kernel sorts the chunks it can and lists the
       // others; persistent comparison-sort CTAs take the list.
       using BF = BucketFor<K, PAIRS>;
@@ -170,17 +250,18 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
         break;
       }
       bucket_kernel<<<static_cast<unsigned>(tiles), BCfg::NT, kBSmem, stream>>>(
-          keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min, W.fallback,
+          keys, vals, O, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min, W.fallback,
           W.ctr + kCtrFallback, W.max_fallback);
       const int lo = occupancy(list_kernel, Cfg::NT, Cfg::kSmemBytes, list_occ, dev);
       const unsigned lgrid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, tiles));
       list_kernel<<<lgrid, Cfg::NT, Cfg::kSmemBytes, stream>>>(
-          keys, vals, off, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
+          keys, vals, O, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
           W.max_fallback);
+      rec.tile_launches = 2;
     } else {
       tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
-          keys, vals, off, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
+          keys, vals, O, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
     }
     if (prof) rec.t1 = prof_event(stream);
     if (cudaGetLastError() != cudaSuccess) {
@@ -188,38 +269,17 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       break;
     }
 
-    // ---- long segments: radix passes, then merge passes, in one cooperative
-    // kernel (returns at once without long segments) ----------------------------------
-    using MS = LongSmem<K, PAIRS>;
-    auto merge_kernel = long_segment_kernel<K, PAIRS, SingleSpace<K>>;
-    static std::atomic<uint64_t> merge_attr_done{0};
-    static std::atomic<int> merge_occ[kMaxDevices];
-    if (!S->coop || ensure_smem(merge_kernel, MS::kBytes, merge_attr_done, dev) != cudaSuccess) {
-      rc = SEGSORT_ERR_CUDA;
-      break;
-    }
-    // All resident CTAs, but no more than one per merge item of the whole
-    // problem: small calls then leave the rest of the GPU to other work.
-    const int mo = occupancy(merge_kernel, kMThreads, MS::kBytes, merge_occ, dev);
-    const int per_sm = R.merge_per_sm > 0 ? std::min(R.merge_per_sm, mo) : mo;
-    const int64_t items = n / MergeShape<K>::T + 1;
-    const unsigned merge_grid =
-        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(per_sm) * S->sms, items));
+    // ---- long segments: radix passes, then merge passes ----------------------
     if (prof) rec.l0 = prof_event(stream);
-    {
-      SingleSpace<K> sp{keys, vals, W.tmp_keys, W.tmp_vals};
-      int64_t cap = tile_cap<K>();
-      void *args[] = {&sp, &W, &cap};
-      if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(merge_kernel), dim3(merge_grid),
-                                      dim3(kMThreads), args, MS::kBytes, stream) != cudaSuccess) {
-        rc = SEGSORT_ERR_CUDA;
-        break;
-      }
-    }
+    rc = launch_long(W);
+    if (rc != SEGSORT_OK) break;
     if (prof) rec.l1 = prof_event(stream);
   } while (false);
   if (prof) {
-    rec.large_launches = 2;  // classify, the cooperative merge-pass kernel
+    // classify and the cooperative long-segment kernel; with the MSD route
+    // also the first classify and long-segment kernel and the three
+    // expansion kernels.
+    rec.large_launches = msd ? 7 : 2;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     g_prof_pending.push_back(rec);
   }
@@ -538,6 +598,10 @@ int segsort_set_param(int param, int64_t value) {
       if (value < 0) return SEGSORT_ERR_INVALID_ARG;
       g_bucket_min_avg.store(value, std::memory_order_relaxed);
       return SEGSORT_OK;
+    case SEGSORT_PARAM_MSD:
+      if (value != 0 && value != 1) return SEGSORT_ERR_INVALID_ARG;
+      g_msd_on.store(value, std::memory_order_relaxed);
+      return SEGSORT_OK;
     default:
       return SEGSORT_ERR_INVALID_ARG;
   }
@@ -554,6 +618,9 @@ int segsort_get_param(int param, int64_t *value) {
       return SEGSORT_OK;
     case SEGSORT_PARAM_BUCKET_MIN_AVG:
       *value = g_bucket_min_avg.load(std::memory_order_relaxed);
+      return SEGSORT_OK;
+    case SEGSORT_PARAM_MSD:
+      *value = g_msd_on.load(std::memory_order_relaxed);
       return SEGSORT_OK;
     default:
       return SEGSORT_ERR_INVALID_ARG;
@@ -700,11 +767,12 @@ int segsort_profile_read(double *tile_ms, double *large_ms, int64_t *tile_launch
   };
   for (PhaseRecord &r : g_prof_pending) {
     g_prof_tile_ms += span(r.t0, r.t1);
-    g_prof_tile_launches += 1;
+    g_prof_tile_launches += r.tile_launches;
     if (r.l0 || r.l1) {
       g_prof_large_ms += span(r.l0, r.l1);
       g_prof_large_launches += r.large_launches;
     }
+    if (r.m0 || r.m1) g_prof_large_ms += span(r.m0, r.m1);
   }
   g_prof_pending.clear();
   if (tile_ms) *tile_ms = g_prof_tile_ms;

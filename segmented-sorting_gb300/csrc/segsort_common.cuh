@@ -59,11 +59,20 @@ template <> struct KeyOrder<uint64_t> {
 // hold nseg and the end of the last segment is n.  Every value is clamped into
 // [0, n], so malformed offsets cannot address memory outside the arrays.
 // ---------------------------------------------------------------------------
+constexpr uint8_t kSegSkip = 0x80;
+constexpr uint8_t kSegShared = 0x7F;
+
 struct Offsets {
   const int32_t *p;
   int32_t nseg;
   int32_t heads;  // 1: heads-only array of nseg entries
   int64_t n;
+  // Optional per-segment flags (null for the caller's offsets): kSegSkip
+  // marks a segment already sorted (one the radix passes finished before the
+  // rest of the call; classify gives it no job); the low bits are the number
+  // of leading order bits every key of the segment shares (a hint for the
+  // bucket sort's scaling).
+  const uint8_t *flags = nullptr;
 
   __device__ __forceinline__ int64_t operator()(int64_t i) const {
     int64_t v = (heads && i >= nseg) ? n : static_cast<int64_t>(__ldg(p + i));

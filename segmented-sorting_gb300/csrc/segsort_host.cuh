@@ -20,6 +20,7 @@
 #include "classify.cuh"
 #include "merge_sort.cuh"
 #include "radix_sort.cuh"
+#include "msd_route.cuh"
 
 namespace segsort {
 
@@ -67,12 +68,13 @@ constexpr int64_t tile_cap() {
 // radix job spans at least two tiles and the job count stays within the
 // layout's bound) nor the tile capacity.  Run-time parameter
 // (segsort_set_param).  Defaults measured on GB300 over 2^24 uint32 pairs in
-// equal segments: the radix route takes 0.58-0.72 ms whatever the length,
-// the merge route 0.45 ms at 2^13 growing to 1.03 ms at 2^20; they meet at
-// 2^15.  64-bit keys need twice the radix passes.
+// equal segments: the LSD radix route takes about 0.62 ms whatever the
+// length, the MSD route (msd_route.cuh) 0.52-0.60 ms from 2^17 up, the merge
+// route over bucket-sorted runs 0.27 ms at 2^13, 0.49 ms at 2^16, 0.58 ms
+// at 2^17 and 0.66 ms at 2^18.  64-bit keys need twice the radix passes.
 constexpr int64_t kRadixTile = static_cast<int64_t>(kRBuckets) * kRItems;
 constexpr int64_t kRadixMinFloor = kRadixTile;
-inline std::atomic<int64_t> g_radix_min32{int64_t{1} << 15};
+inline std::atomic<int64_t> g_radix_min32{int64_t{1} << 16};
 inline std::atomic<int64_t> g_radix_min64{int64_t{1} << 18};
 
 template <typename K>
@@ -99,6 +101,11 @@ inline std::atomic<int64_t> g_stream_max_avg{32};
 // segment the comparison sort is faster (measured on GB300, 2^24 u32 pairs:
 // 0.20 against 0.25 ms at 64, even at 128).  Run-time parameter.
 inline std::atomic<int64_t> g_bucket_min_avg{128};
+
+// Problems whose average segment is longer than the radix threshold take
+// the MSD route for their radix segments (msd_route.cuh) when this is set
+// and the library owns the workspace.  Run-time parameter.
+inline std::atomic<int64_t> g_msd_on{1};
 
 // ---------------------------------------------------------------------------
 // Route of one plain call: the radix threshold, the streamed-tile threshold
@@ -263,6 +270,8 @@ inline LargeWs<K> ws_views(unsigned char *base, const WsLayout &L) {
   W.halves = L.halves;
   W.max_rtiles = L.max_rtiles;
   W.radix_min = L.radix_min;
+  W.msd_stage = 0;
+  W.tile_cap = static_cast<int32_t>(tile_cap<K>());
   return W;
 }
 

@@ -523,15 +523,11 @@ __device__ __forceinline__ void sort_chunk(const K *src_keys, const uint32_t *sr
 template <typename Cfg, bool PAIRS, typename K, bool kShort, typename Dst>
 __device__ __forceinline__ void sort_loaded(Dst &&dst, int m, bool multi, unsigned char *smem,
                                             uint32_t *hb, int *warp_s) {
-  using Ord = typename Cfg::Ord;
   using WT = typename Cfg::WT;
   using Word = typename Cfg::Word;
   constexpr int NT = Cfg::NT;
   constexpr int KPT = Cfg::KPT;
   Word *W = reinterpret_cast<Word *>(smem);
-  K *KO = reinterpret_cast<K *>(smem);
-  uint32_t *VO = reinterpret_cast<uint32_t *>(smem + Cfg::OSLOTS * sizeof(K));
-  uint32_t *Vs = reinterpret_cast<uint32_t *>(smem + Cfg::kMainBytes);
   const int tid = threadIdx.x;
   const int base = tid * KPT;
 
