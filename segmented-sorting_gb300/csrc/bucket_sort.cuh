@@ -119,87 +119,61 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
   uint16_t *SB = reinterpret_cast<uint16_t *>(smem + BL::kBkt);
   uint32_t *CN = reinterpret_cast<uint32_t *>(smem + BL::kCnt);
 
-  // ---- keys and values to registers (position q * NT + tid); the chunk's
-  // AND and OR of the order bits ------------------------------------------------
+  // Per-segment flags (the MSD route's second stage): the order bits a
+  // segment's keys share, which are shifted out too so that its keys spread
+  // over its buckets, and whether the segment's keys are in the temporary
+  // buffers (the MSD pass left them there).  Per head position in SH (over
+  // the bucket indices' region, unused until the scatter).
+  const bool hinted = off.flags != nullptr;
+  uint8_t *SH = reinterpret_cast<uint8_t *>(smem + BL::kBkt);
+  const uint8_t one_flag = hinted && !multi ? off.flags[C.lo] : 0;
+
+  // Segment [s, t) of chunk position i (multi: from the head bitmask).
+  auto bounds = [&](int i, int &s, int &t) {
+    const int w = i >> 5, bit = i & 31;
+    const uint32_t x = hb[w];
+    const uint32_t below = x & (0xFFFFFFFFu >> (31 - bit));
+    s = below ? (w << 5) + 31 - __clz(below) : max(hprev[w], 0);
+    const uint32_t above = bit == 31 ? 0u : x & (0xFFFFFFFEu << bit);
+    t = above ? (w << 5) + __ffs(above) - 1 : hnext[w];
+  };
+  // ---- keys and values to registers (position q * NT + tid), each from the
+  // buffer its segment is in: first all from the buffer of the chunk's first
+  // segment (in flight during the head phase), then, for a chunk of several
+  // segments, again from the other buffer where a segment's flag says so
+  // (only chunks that straddle an MSD segment's end) --------------------------------
   Bits kb[IPT];
   uint32_t kv[IPT];
-  Bits band = ~Bits(0), bor = 0;
+  const bool spec_tmp = hinted && ((multi ? off.flags[C.lo] : one_flag) & kSegTmp) != 0;
+  bool any_tmp = spec_tmp && m > 0;
+  {
+    const K *sk = (spec_tmp ? tmp_keys : keys) + C.a;
+    const uint32_t *sv = PAIRS ? (spec_tmp ? tmp_vals : vals) + C.a : nullptr;
 #pragma unroll
-  for (int q = 0; q < IPT; ++q) {
-    const int i = q * NT + tid;
-    kb[q] = 0;
-    kv[q] = 0;
-    if (i < m) {
-      kb[q] = Ord::to_bits(io.src_keys[i]);
-      if constexpr (PAIRS) kv[q] = io.src_vals[i];
-      band &= kb[q];
-      bor |= kb[q];
+    for (int q = 0; q < IPT; ++q) {
+      const int i = q * NT + tid;
+      kb[q] = 0;
+      kv[q] = 0;
+      if (i < m) {
+        kb[q] = Ord::to_bits(sk[i]);
+        if constexpr (PAIRS) kv[q] = sv[i];
+      }
     }
   }
   __syncthreads();  // earlier readers of the shared memory are done
   for (int i = tid; i < BL::kCntSlots; i += NT) CN[i] = 0u;
   if (multi)
     for (int i = tid; i < HW; i += NT) hb[i] = 0u;
-  {
-    const uint32_t a0 = __reduce_and_sync(0xFFFFFFFFu, static_cast<uint32_t>(band));
-    const uint32_t o0 = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(bor));
-    uint32_t a1 = 0, o1 = 0;
-    if constexpr (sizeof(Bits) == 8) {
-      a1 = __reduce_and_sync(0xFFFFFFFFu, static_cast<uint32_t>(static_cast<uint64_t>(band) >> 32));
-      o1 = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(static_cast<uint64_t>(bor) >> 32));
-    }
-    if (lane == 0) {
-      red_s[0][warp] = a0;
-      red_s[1][warp] = a1;
-      red_s[2][warp] = o0;
-      red_s[3][warp] = o1;
-    }
-  }
-  __syncthreads();
-  Bits all_and = ~Bits(0), all_or = 0;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    Bits a = red_s[0][w], o = red_s[2][w];
-    if constexpr (sizeof(Bits) == 8) {
-      a |= static_cast<Bits>(red_s[1][w]) << 32;
-      o |= static_cast<Bits>(red_s[3][w]) << 32;
-    }
-    all_and &= a;
-    all_or |= o;
-  }
-  const Bits varying = all_and ^ all_or;  // bits that are not the same in every key
-  if (varying == 0) {
-    // Every key is equal: the stable order is the input order.
-    if (io.dst_keys != io.src_keys) {
-#pragma unroll
-      for (int q = 0; q < IPT; ++q) {
-        const int i = q * NT + tid;
-        if (i < m) {
-          io.dst_keys[i] = Ord::from_bits(kb[q]);
-          if constexpr (PAIRS) io.dst_vals[i] = kv[q];
-        }
-      }
-    }
-    __syncthreads();
-    return true;
-  }
-  const int sh = leading_zeros(varying);
-  // Order bits the keys of a segment share, when the offsets say (the MSD
-  // route's sub-buckets): shifted out too, so that the segment's keys spread
-  // over its buckets.  Per head position in SH (over the bucket indices'
-  // region, unused until the scatter).
-  uint8_t *SH = reinterpret_cast<uint8_t *>(smem + BL::kBkt);
-  const bool hinted = off.flags != nullptr;
-  const int seg_sh = hinted && !multi ? (off.flags[C.lo] & kSegShared) : 0;
   // ---- segment heads; per head word the last head before it and the first
   // after it ------------------------------------------------------------------------
   if (multi) {
+    __syncthreads();  // cleared head words
     for (int64_t j = C.lo + tid; j < C.hi; j += NT) {
       const int64_t b0 = off(j);
       const int64_t p = b0 - C.a;
       if (p >= 0 && p < m) {
         atomicOr(&hb[p >> 5], 1u << (p & 31));
-        if (hinted && off(j + 1) > b0) SH[p] = off.flags[j] & kSegShared;
+        if (hinted && off(j + 1) > b0) SH[p] = off.flags[j];
       }
     }
     __syncthreads();
@@ -241,6 +215,87 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     }
     __syncthreads();
   }
+  if (hinted && multi) {
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+      const int i = q * NT + tid;
+      if (i < m) {
+        int s0, t0;
+        bounds(i, s0, t0);
+        const bool in_tmp = (SH[s0] & kSegTmp) != 0;
+        if (in_tmp != spec_tmp) {
+          kb[q] = Ord::to_bits((in_tmp ? tmp_keys : keys)[C.a + i]);
+          if constexpr (PAIRS) kv[q] = (in_tmp ? tmp_vals : vals)[C.a + i];
+        }
+        any_tmp |= in_tmp;
+      }
+    }
+  }
+  // The chunk's AND and OR of the order bits.
+  Bits band = ~Bits(0), bor = 0;
+#pragma unroll
+  for (int q = 0; q < IPT; ++q) {
+    if (q * NT + tid < m) {
+      band &= kb[q];
+      bor |= kb[q];
+    }
+  }
+  {
+    const uint32_t a0 = __reduce_and_sync(0xFFFFFFFFu, static_cast<uint32_t>(band));
+    const uint32_t o0 = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(bor));
+    uint32_t a1 = 0, o1 = 0;
+    if constexpr (sizeof(Bits) == 8) {
+      a1 = __reduce_and_sync(0xFFFFFFFFu, static_cast<uint32_t>(static_cast<uint64_t>(band) >> 32));
+      o1 = __reduce_or_sync(0xFFFFFFFFu, static_cast<uint32_t>(static_cast<uint64_t>(bor) >> 32));
+    }
+    if (lane == 0) {
+      red_s[0][warp] = a0;
+      red_s[1][warp] = a1;
+      red_s[2][warp] = o0;
+      red_s[3][warp] = o1;
+    }
+  }
+  // Some key came from the temporary buffers: a refusal must leave the chunk
+  // in the caller's, where the comparison sort reads it.
+  const bool from_tmp = hinted && __syncthreads_or(any_tmp);
+  if (!hinted) __syncthreads();
+  auto write_back = [&](bool to_tmp) {
+    K *dk = (to_tmp ? tmp_keys : keys) + C.a;
+    uint32_t *dv = PAIRS ? (to_tmp ? tmp_vals : vals) + C.a : nullptr;
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+      const int i = q * NT + tid;
+      if (i < m) {
+        dk[i] = Ord::from_bits(kb[q]);
+        if constexpr (PAIRS) dv[i] = kv[q];
+      }
+    }
+  };
+  Bits all_and = ~Bits(0), all_or = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    Bits a = red_s[0][w], o = red_s[2][w];
+    if constexpr (sizeof(Bits) == 8) {
+      a |= static_cast<Bits>(red_s[1][w]) << 32;
+      o |= static_cast<Bits>(red_s[3][w]) << 32;
+    }
+    all_and &= a;
+    all_or |= o;
+  }
+  const Bits varying = all_and ^ all_or;  // bits that are not the same in every key
+  if (varying == 0) {
+    // Every key is equal: the stable order is the input order.
+    if (from_tmp || C.tmp) write_back(C.tmp != 0);
+    __syncthreads();
+    return true;
+  }
+  if (hinted && static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg > m) {
+    // Short segments: the comparison sort is faster.
+    if (from_tmp) write_back(false);
+    return false;
+  }
+  const int sh = leading_zeros(varying);
+  const int seg_sh = one_flag & kSegShared;
   // ---- bucket of every key; count (the old count is the key's slot) ----------------
   uint32_t pk[IPT];
 #pragma unroll
@@ -249,17 +304,10 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     pk[q] = 0;
     if (i < m) {
       int s = 0, t = m;
-      if (multi) {
-        const int w = i >> 5, bit = i & 31;
-        const uint32_t x = hb[w];
-        const uint32_t below = x & (0xFFFFFFFFu >> (31 - bit));
-        s = below ? (w << 5) + 31 - __clz(below) : max(hprev[w], 0);
-        const uint32_t above = bit == 31 ? 0u : x & (0xFFFFFFFEu << bit);
-        t = above ? (w << 5) + __ffs(above) - 1 : hnext[w];
-      }
+      if (multi) bounds(i, s, t);
       const uint32_t len = t > s ? static_cast<uint32_t>(t - s) : 1u;
       int shift = sh;
-      if (hinted) shift = max(shift, multi ? static_cast<int>(SH[s]) : seg_sh);
+      if (hinted) shift = max(shift, multi ? static_cast<int>(SH[s] & kSegShared) : seg_sh);
       shift = min(shift, static_cast<int>(8 * sizeof(Bits)) - 1);
       int b = s + static_cast<int>(bucket_scale<Bits>(kb[q] << shift, len));
       b = b < 0 ? 0 : (b >= m ? m - 1 : b);  // only malformed offsets reach the clamp
@@ -303,7 +351,10 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     sq_all += red_s[0][w];
     mx_all = max(mx_all, red_s[1][w]);
   }
-  if (sq_all > kBucketSkew * static_cast<uint32_t>(m) || mx_all > kBucketMaxSize) return false;
+  if (sq_all > kBucketSkew * static_cast<uint32_t>(m) || mx_all > kBucketMaxSize) {
+    if (from_tmp) write_back(false);
+    return false;
+  }
   // ---- scatter to the buckets --------------------------------------------------------
 #pragma unroll
   for (int q = 0; q < IPT; ++q) {
@@ -382,7 +433,9 @@ tile_bucket_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
   const int nc = plan_s.nc;
   for (int c = 0; c < nc; ++c) {
     const TileChunk &C = plan_s.c[c];
-    if (static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg <= C.m &&
+    // With segment flags the body loads every chunk (some keys may be in the
+    // temporary buffers) and makes the short-segment test itself.
+    if ((off.flags != nullptr || static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg <= C.m) &&
         bucket_sort_body<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s))
       continue;
     if (threadIdx.x == 0) {

@@ -7,10 +7,10 @@
 // instead of one LSD pass per varying digit:
 //   stage 1  the long-segment kernel with LargeWs::msd_stage set: the counts
 //            and bucket starts as for the LSD passes, then one stable counting
-//            pass on that top digit for these segments (all their passes for
-//            the other radix segments), the copy back, and no merge passes.
-//            The segment is now its 256 sub-buckets in order, each holding
-//            its keys in their input order.
+//            pass on that top digit for these segments (all their passes and
+//            the copy back for the other radix segments), and no merge
+//            passes.  The segment is now its 256 sub-buckets in order, each
+//            holding its keys in their input order, in the temporary buffers.
 //   expand   (this file) the offsets of a second problem over the same keys:
 //            every segment as it was, except that an MSD segment becomes its
 //            sub-buckets (flagged with the order bits their keys share: the
@@ -18,12 +18,15 @@
 //            sort shifts out) and a radix segment stage 1 finished is marked
 //            skip.
 //   stage 2  the usual launch sequence over those offsets: classify (no jobs
-//            for skipped segments), the tile sort (sub-buckets of at most a
-//            tile, and the short segments), the long-segment kernel (merge
-//            passes for the rest).
-// For 32-bit keys that is 4 bytes per key for the counts and 16 + 16 + 16
-// bytes per pair for the pass, the copy back and the tile sort, against
-// 4 + 4 * 16 for four LSD passes.  The output is the stable sort of every
+//            for skipped segments), the bucket route of the tile sort (it
+//            reads a sub-bucket from the temporary buffers and writes it to
+//            the caller's, or to the buffer the first merge pass reads for the
+//            CAP-runs of a sub-bucket longer than a tile; a chunk it refuses
+//            it first copies to the caller's buffers for the comparison
+//            sort), the long-segment kernel (merge passes for the rest).
+// For 32-bit keys that is 4 bytes per key for the counts and 16 + 16 bytes
+// per pair for the pass and the tile sort, against 4 + 4 * 16 for four LSD
+// passes.  The output is the stable sort of every
 // segment either way (the pass is stable and the sub-buckets are sorted
 // stably), so the route changes nothing in the result.
 //
@@ -131,7 +134,7 @@ __global__ void __launch_bounds__(kRBuckets) msd_sub_kernel(LargeWs<K> ws, MsdWs
   const uint32_t st = ws.rhist[(static_cast<int64_t>(q) * D + dt) * kRBuckets + g];
   if (at >= 0 && at < M.c_len) {
     M.sub[at] = jb.x + static_cast<int32_t>(st);
-    M.flags[at] = static_cast<uint8_t>(8 * (D - dt));
+    M.flags[at] = static_cast<uint8_t>(8 * (D - dt)) | kSegTmp;
   }
 }
 

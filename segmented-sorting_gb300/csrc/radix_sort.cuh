@@ -450,8 +450,10 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
 #pragma unroll
       for (int w = 0; w < NW; ++w) mx = max(mx, static_cast<uint32_t>(warp_s[w]));
       __syncthreads();
-      if (mx <= static_cast<uint32_t>(kMsdMaxBucketTiles * ws.tile_cap))
-        varying = (1u << dt) | kRDigitMsd;
+      // (A sub-bucket must stay at most the radix threshold: the second
+      // stage gives longer ones radix passes, which read the caller's buffers.)
+      const int64_t lim = min(static_cast<int64_t>(kMsdMaxBucketTiles) * ws.tile_cap, ws.radix_min);
+      if (mx <= static_cast<uint64_t>(lim)) varying = (1u << dt) | kRDigitMsd;
     }
     if (tid == 0) {
       ws.rdigits[j] = varying;
@@ -659,7 +661,10 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
   // ---- segments that ran an odd number of passes: tmp -> caller ------------
   for (int64_t t = blockIdx.x; t < ntiles; t += G) {
     const int4 de = ws.rtile_desc[t];
-    if (!(__popc(ws.rdigits[de.z] & kRDigitMask) & 1)) continue;
+    // (Not the MSD route's segments: their second stage reads the temporary
+    // buffers.)
+    const uint32_t v = ws.rdigits[de.z];
+    if (!(__popc(v & kRDigitMask) & 1) || (v & kRDigitMsd)) continue;
     const int cnt = de.y;
     const SideBuffers<K> B = sp(ws.rjobs[de.z].w);
     K kk[IPT];

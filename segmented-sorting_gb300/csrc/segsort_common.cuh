@@ -59,8 +59,9 @@ template <> struct KeyOrder<uint64_t> {
 // hold nseg and the end of the last segment is n.  Every value is clamped into
 // [0, n], so malformed offsets cannot address memory outside the arrays.
 // ---------------------------------------------------------------------------
-constexpr uint8_t kSegSkip = 0x80;
-constexpr uint8_t kSegShared = 0x7F;
+constexpr uint8_t kSegSkip = 0x80;    // already sorted
+constexpr uint8_t kSegTmp = 0x40;     // its keys and values are in the temporary buffers
+constexpr uint8_t kSegShared = 0x3F;  // leading order bits its keys share
 
 struct Offsets {
   const int32_t *p;
@@ -69,9 +70,11 @@ struct Offsets {
   int64_t n;
   // Optional per-segment flags (null for the caller's offsets): kSegSkip
   // marks a segment already sorted (one the radix passes finished before the
-  // rest of the call; classify gives it no job); the low bits are the number
-  // of leading order bits every key of the segment shares (a hint for the
-  // bucket sort's scaling).
+  // rest of the call; classify gives it no job); kSegTmp a segment whose keys
+  // and values are in the temporary buffers (only the bucket kernel reads
+  // them there; the result goes to the caller's buffers); the low bits the
+  // number of leading order bits every key of the segment shares (a hint
+  // for the bucket sort's scaling).
   const uint8_t *flags = nullptr;
 
   __device__ __forceinline__ int64_t operator()(int64_t i) const {
