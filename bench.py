@@ -589,6 +589,8 @@ def run_ours(args) -> None:
     cap = 4096  # tile capacity of 32-bit keys: longer segments take a long-segment route
     radix_min = pkg.get_param(pkg.PARAM_RADIX_MIN_32)
     stream_max_avg = pkg.get_param(pkg.PARAM_STREAM_MAX_AVG)
+    bucket_min_avg = pkg.get_param(pkg.PARAM_BUCKET_MIN_AVG)
+    msd_on = pkg.get_param(pkg.PARAM_MSD)
     launches_per_step = sum(p["tile_launches"] + p["large_launches"] for p in phase.values())
 
     def merge_passes(length: int) -> int:
@@ -597,49 +599,73 @@ def run_ours(args) -> None:
             runs, p = (runs + 1) // 2, p + 1
         return p
 
-    def varying_digits(lg: int) -> int:
+    def varying_digits(lg: int) -> list[int]:
         """8-bit digit positions whose value differs somewhere inside a
         segment of the instance: the radix passes the library runs."""
         k = pristine[lg].long() & 0xFFFFFFFF
         seg = torch.arange(n, device=dev) >> lg
-        count = 0
+        out = []
         for d in range(4):
             dg = (k >> (8 * d)) & 255
             lo = torch.full((n >> lg,), 256, dtype=torch.long, device=dev).scatter_reduce(
                 0, seg, dg, reduce="amin")
             hi = torch.full((n >> lg,), -1, dtype=torch.long, device=dev).scatter_reduce(
                 0, seg, dg, reduce="amax")
-            count += int(bool((lo != hi).any()))
-        return count
+            if bool((lo != hi).any()):
+                out.append(d)
+        return out
 
-    # Algorithmic bytes per launch.  The tile kernel reads and writes every
-    # key and value once and reads the offsets: all of them when the segments
-    # are at most a tile long, the long segments' elements when it forms their
-    # sorted runs for the merge passes.  A merge pass reads and writes every key
-    # and value of its segments once.  The radix route reads every key once
-    # for the digit counts, then reads and writes every key and value once per
-    # digit position that varies, plus one copy back after an odd number of
-    # passes.  The library runs the streamed tile kernel when the average
-    # segment is at most stream_max_avg long, the one-CTA-per-tile kernel
-    # otherwise.
-    tile_bytes, stream_bytes, long_bytes, idle_tile = {}, {}, {}, []
+    def msd_oversize_keys(lg: int, d: int) -> int:
+        """Keys in sub-buckets (segment, value of digit d) longer than a tile:
+        the MSD route's second stage gives them one merge pass (sub-buckets
+        are at most two tiles long)."""
+        k = pristine[lg].long() & 0xFFFFFFFF
+        sub = ((torch.arange(n, device=dev) >> lg) << 8) | ((k >> (8 * d)) & 255)
+        c = torch.bincount(sub, minlength=(n >> lg) << 8)
+        return int(c[c > cap].sum())
+
+    # Algorithmic bytes per launch.  The tile kernels read and write every
+    # key and value once and read the offsets: all of them when the segments
+    # are at most a tile long, the long segments' elements when they form
+    # their sorted runs for the merge passes.  A merge pass reads and writes
+    # every key and value of its segments once.  The LSD radix route reads
+    # every key once for the digit counts, then reads and writes every key and
+    # value once per digit position that varies, plus one copy back after an
+    # odd number of passes.  The MSD route (segments longer than the radix
+    # threshold whose keys vary in at least three digits) reads every key for
+    # the counts and every pair once in its one pass (long-segment kernel),
+    # then every pair once in the bucket kernel, plus a merge pass over the
+    # sub-buckets longer than a tile.  The library runs the streamed tile
+    # kernel when the average segment is at most stream_max_avg long, the
+    # bucket route (tile_bucket_kernel, and tile_list_kernel for the chunks it
+    # refuses) from bucket_min_avg on, the one-CTA-per-tile comparison sort
+    # between.
+    tile_bytes, stream_bytes, bucket_bytes, long_bytes, idle_tile = {}, {}, {}, {}, []
     for lg in lengths:
         ln = 1 << lg
         full = BYTES_PER_PAIR * n + 4 * (n // ln + 1)
+        tile_table = bucket_bytes if bucket_min_avg and ln >= bucket_min_avg else tile_bytes
         if ln <= stream_max_avg:
             stream_bytes[lg] = full
         elif ln <= cap:
-            tile_bytes[lg] = full
+            tile_table[lg] = full
         elif ln <= radix_min:
-            tile_bytes[lg] = full
+            tile_table[lg] = full
             long_bytes[lg] = BYTES_PER_PAIR * n * merge_passes(ln)
         else:
-            idle_tile.append(lg)  # the tile kernel finds no work: every segment is on the radix route
-            passes = varying_digits(lg)
-            long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n * (passes + (passes & 1))
+            digits = varying_digits(lg)
+            if msd_on and len(digits) >= 3:
+                bucket_bytes[lg] = BYTES_PER_PAIR * n
+                long_bytes[lg] = (4 * n + BYTES_PER_PAIR * n
+                                  + BYTES_PER_PAIR * msd_oversize_keys(lg, digits[-1]))
+            else:
+                idle_tile.append(lg)  # the tile kernel finds no work: every segment is on the radix route
+                passes = len(digits)
+                long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n * (passes + (passes & 1))
     kernels = {}
     for name, table, key in (("tile_sort_kernel", tile_bytes, "tile_ms"),
                              ("tile_stream_kernel", stream_bytes, "tile_ms"),
+                             ("tile_bucket_kernel", bucket_bytes, "tile_ms"),
                              ("long_segment_kernel", long_bytes, "large_ms")):
         ms_sum = sum(phase[lg][key] for lg in table)
         byts = sum(table.values())
@@ -663,6 +689,7 @@ def run_ours(args) -> None:
                 "traffic": ((tr or {}).get(name) or {}).get("dram_bytes_per_launch"),
                 "traffic_workload": ((tr or {}).get(name) or {}).get("workload"),
                 "radix_min": radix_min, "stream_max_avg": stream_max_avg,
+                "bucket_min_avg": bucket_min_avg, "msd": msd_on,
                 "kernels": kernels}
 
     # ---- end to end through the public API with host buffers ---------------
