@@ -365,7 +365,20 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
                        "plain_ms": round(statistics.median(t_p), 4)}
         return out
 
+    def plain_launches() -> int:
+        """Kernels one pass of plain calls launches (the library's phase
+        records: tile-sort and long-segment launches of every call)."""
+        pkg.profile_enable(True)
+        pkg.profile_read(reset=True)
+        restore()
+        plain()
+        torch.cuda.synchronize()
+        p = pkg.profile_read(reset=True)
+        pkg.profile_enable(False)
+        return int(p["tile_launches"] + p["large_launches"])
+
     try:
+        n_plain_launches = plain_launches()
         t_plain = _timed(stream, plain, restore, warmup, steps)
         ref = [(r["k"].clone(), r["v"].clone()) for r in rows]
         t_one = _timed(stream, one_shot, restore, warmup, steps)
@@ -394,7 +407,9 @@ def bench_batched(pkg, inst, dev, stream, warmup: int, steps: int) -> dict:
         "plan_p99_ms": round(float(np.percentile(t_plan, 99)), 4),
         "identical_to_plain": identical, "plan_workspace_bytes": ws, "steps": steps,
         "tuned_merge_ctas_per_sm": tuned.value, "by_key_type": groups,
-        "launches": {"plain": 3 * len(specs), "plan_graph": 3 * len(types)},
+        # per key-type group: classify, the bucket kernel, the list kernel,
+        # the long-segment kernel
+        "launches": {"plain": n_plain_launches, "plan_graph": 4 * len(types)},
     }
 
 

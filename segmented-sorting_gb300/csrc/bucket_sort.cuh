@@ -35,6 +35,11 @@
 
 namespace segsort {
 
+// Shortest average segment of a chunk the bucket sort is tried on: below it
+// the comparison sort is faster (its merge levels stop at the segment length;
+// on GB300, 2^24 u32 pairs: 0.20 against 0.25 ms at 64 keys per segment, even
+// at 128).
+constexpr int64_t kBucketMinAvg = 128;
 constexpr uint32_t kBucketSkew = 3;      // sum of squared bucket sizes <= 3 m
 constexpr uint32_t kBucketMaxSize = 24;  // largest bucket a thread ranks alone
 // Buckets up to this size are ranked by an unrolled loop of this many
@@ -77,12 +82,6 @@ struct BucketLayout {
   static constexpr size_t kBytes = kCnt + kCntSlots * sizeof(uint32_t);
   static __device__ __forceinline__ int cslot(int b) { return b + (b >> 5); }
 };
-
-template <typename Cfg, bool PAIRS>
-constexpr size_t tile_smem_bytes() {
-  return Cfg::kSmemBytes > BucketLayout<Cfg, PAIRS>::kBytes ? Cfg::kSmemBytes
-                                                             : BucketLayout<Cfg, PAIRS>::kBytes;
-}
 
 // Sorts chunk C by buckets, or returns false (uniformly over the CTA) having
 // written nothing.  Every thread of the CTA calls it; hb is the tile
@@ -396,16 +395,6 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
   return true;
 }
 
-// The same, not inlined, for the comparison-sort kernels that try it first
-// (the batched tile kernel).
-template <typename Cfg, bool PAIRS, typename K>
-__device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint32_t *vals,
-                                               const Offsets &off, K *tmp_keys,
-                                               uint32_t *tmp_vals, unsigned char *smem,
-                                               uint32_t *hb, int *warp_s) {
-  return bucket_sort_body<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s);
-}
-
 // ---------------------------------------------------------------------------
 // The bucket route of the tile sort: two kernels.  tile_bucket_kernel: CTA t
 // plans tile t (plan_tile) and bucket-sorts its chunks; a chunk of segments
@@ -414,18 +403,21 @@ __device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint
 // listed chunks with the comparison sort (its own launch shape: 256 threads,
 // 128 registers).  The list holds at most kMaxTileChunks chunks per tile.
 // ---------------------------------------------------------------------------
-template <typename K, bool PAIRS, int NT, int KPT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-tile_bucket_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
-                   const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
-                   uint32_t *__restrict__ tmp_vals, int64_t radix_min, TileChunk *fallback,
-                   uint32_t *fallback_count, int64_t max_fallback) {
+// One CTA of the bucket kernel: tile t of a problem (instance inst of a
+// batch) whose half-tile map is half_first.
+template <typename K, bool PAIRS, int NT, int KPT>
+__device__ __forceinline__ void bucket_tile(K *__restrict__ keys, uint32_t *__restrict__ vals,
+                                            const Offsets &off,
+                                            const int32_t *__restrict__ half_first, int64_t t,
+                                            K *__restrict__ tmp_keys,
+                                            uint32_t *__restrict__ tmp_vals, int64_t radix_min,
+                                            TileChunk *fallback, uint32_t *fallback_count,
+                                            int64_t max_fallback, int32_t inst) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ TilePlan plan_s;
   __shared__ uint32_t hb[Cfg::CAP / 32];
   __shared__ int warp_s[NT / 16];
-  const int64_t t = blockIdx.x;
   if (t * Cfg::CAP >= off.n) return;
   if (threadIdx.x == 0)
     plan_tile<Cfg::CAP>(off, half_first, t, tmp_keys != nullptr, radix_min, plan_s);
@@ -440,9 +432,23 @@ tile_bucket_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
       continue;
     if (threadIdx.x == 0) {
       const uint32_t at = atomicAdd(fallback_count, 1u);
-      if (at < max_fallback) fallback[at] = C;
+      if (at < max_fallback) {
+        TileChunk L = C;
+        L.inst = inst;
+        fallback[at] = L;
+      }
     }
   }
+}
+
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_bucket_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
+                   const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
+                   uint32_t *__restrict__ tmp_vals, int64_t radix_min, TileChunk *fallback,
+                   uint32_t *fallback_count, int64_t max_fallback) {
+  bucket_tile<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x, tmp_keys, tmp_vals,
+                                 radix_min, fallback, fallback_count, max_fallback, 0);
 }
 
 template <typename K, bool PAIRS, int NT, int KPT, int MINB>
@@ -458,6 +464,44 @@ tile_list_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
   for (int64_t i = blockIdx.x; i < c; i += gridDim.x) {
     const TileChunk C = list[i];
     sort_tile_chunk<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s);
+  }
+}
+
+// The batched forms: CTA t of the bucket kernel takes the tile of the last
+// instance whose first tile is at or before t (find_instance, as the batched
+// comparison kernel); the list kernel finds each listed chunk's instance in
+// the chunk.
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_bucket_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
+                         const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
+                         uint32_t *__restrict__ tmp_vals, int64_t radix_min,
+                         TileChunk *fallback, uint32_t *fallback_count, int64_t max_fallback) {
+  const int64_t t = blockIdx.x;
+  const int32_t i = find_instance(tab, count, t, &BatchInst::tile_base);
+  const BatchInst &I = tab[i];
+  bucket_tile<K, PAIRS, NT, KPT>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
+                                 half_first + I.half_base, t - I.tile_base,
+                                 tmp_keys + I.tmp_base, PAIRS ? tmp_vals + I.tmp_base : nullptr,
+                                 radix_min, fallback, fallback_count, max_fallback, i);
+}
+
+template <typename K, bool PAIRS, int NT, int KPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+tile_list_batch_kernel(const BatchInst *__restrict__ tab, K *__restrict__ tmp_keys,
+                       uint32_t *__restrict__ tmp_vals, const TileChunk *__restrict__ list,
+                       const uint32_t *count, int64_t max_list) {
+  using Cfg = TileConfig<K, PAIRS, NT, KPT>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t hb[Cfg::CAP / 32];
+  __shared__ int warp_s[NT / 16];
+  const int64_t c = min(static_cast<int64_t>(*count), max_list);
+  for (int64_t i = blockIdx.x; i < c; i += gridDim.x) {
+    const TileChunk C = list[i];
+    const BatchInst &I = tab[C.inst];
+    sort_tile_chunk<Cfg, PAIRS>(C, static_cast<K *>(I.keys), I.vals, I.offsets_view(),
+                                tmp_keys + I.tmp_base, PAIRS ? tmp_vals + I.tmp_base : nullptr,
+                                smem, hb, warp_s);
   }
 }
 

@@ -146,19 +146,28 @@ cudaError_t upload_table(const std::vector<BatchInst> &v, BatchInst *dst, cudaSt
 template <typename K>
 struct BatchKernels {
   using TCfg = typename TileFor<K, true>::Cfg;
+  using BF = BucketFor<K, true>;
+  using BCfg = typename BF::Cfg;
   using MS = LongSmem<K, true>;
-  static constexpr auto tile = tile_sort_batch_kernel<K, true, TCfg::NT, TCfg::KPT,
+  static constexpr size_t kBSmem = BucketLayout<BCfg, true>::kBytes;
+  // The tile sort: the bucket route (bucket kernel, then the comparison sort
+  // of the chunks it lists), as plain calls of segments of 128 keys or more.
+  static constexpr auto bucket = tile_bucket_batch_kernel<K, true, BCfg::NT, BCfg::KPT,
+                                                          BF::kMinBlocks>;
+  static constexpr auto list = tile_list_batch_kernel<K, true, TCfg::NT, TCfg::KPT,
                                                       TileFor<K, true>::kMinBlocks>;
   static constexpr auto merge = long_segment_kernel<K, true, BatchSpace<K>>;
   static constexpr auto classify = large_classify_halves_batch_kernel<K>;
-  static inline std::atomic<uint64_t> tile_attr{0}, merge_attr{0};
-  static inline std::atomic<int> merge_occ[kMaxDevices];
+  static inline std::atomic<uint64_t> bucket_attr{0}, list_attr{0}, merge_attr{0};
+  static inline std::atomic<int> merge_occ[kMaxDevices], list_occ[kMaxDevices];
 
   // Attributes and occupancy, before any capture.
   static cudaError_t prepare(int dev) {
-    cudaError_t e = ensure_smem(tile, tile_smem_bytes<TCfg, true>(), tile_attr, dev);
+    cudaError_t e = ensure_smem(bucket, kBSmem, bucket_attr, dev);
+    if (e == cudaSuccess) e = ensure_smem(list, TCfg::kSmemBytes, list_attr, dev);
     if (e == cudaSuccess) e = ensure_smem(merge, MS::kBytes, merge_attr, dev);
     if (e == cudaSuccess) occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
+    if (e == cudaSuccess) occupancy(list, TCfg::NT, TCfg::kSmemBytes, list_occ, dev);
     return e;
   }
 
@@ -178,8 +187,15 @@ struct BatchKernels {
 
     // Tile sort first: it forms the sorted runs the merge passes read (the
     // radix passes read the caller's buffers, which it leaves alone).
-    tile<<<static_cast<unsigned>(G.tiles), TCfg::NT, tile_smem_bytes<TCfg, true>(), stream>>>(
-        tab, count, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
+    bucket<<<static_cast<unsigned>(G.tiles), BCfg::NT, kBSmem, stream>>>(
+        tab, count, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min, W.fallback,
+        W.ctr + kCtrFallback, W.max_fallback);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    const int lo = occupancy(list, TCfg::NT, TCfg::kSmemBytes, list_occ, dev);
+    const unsigned lgrid =
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S.sms, G.tiles));
+    list<<<lgrid, TCfg::NT, TCfg::kSmemBytes, stream>>>(tab, W.tmp_keys, W.tmp_vals, W.fallback,
+                                                      W.ctr + kCtrFallback, W.max_fallback);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     const int64_t items = G.total_n / MergeShape<K>::T + 1;

@@ -16,6 +16,7 @@
 #include "segsort.h"
 #include "segsort_common.cuh"
 #include "tile_sort.cuh"
+#include "bucket_sort.cuh"
 #include "tile_stream.cuh"
 #include "classify.cuh"
 #include "merge_sort.cuh"

@@ -722,6 +722,7 @@ constexpr int kMaxTileChunks = 5;
 struct TileChunk {
   int64_t a;
   int32_t lo, hi, m, tmp;
+  int32_t inst = 0;  // instance of a batch (the bucket route's fallback list)
 };
 struct TilePlan {
   TileChunk c[kMaxTileChunks];
@@ -838,30 +839,14 @@ __device__ __forceinline__ void sort_tile_chunk(const TileChunk &C, K *keys, uin
                          smem, hb, warp_s);
 }
 
-// Bucket sort of a chunk (bucket_sort.cuh): false when the chunk's keys are
-// too skewed for it, having written nothing.  Not inlined: the comparison
-// sort of a kernel that tries it first keeps its own register allocation
-// (inlined together, the two spill).
-template <typename Cfg, bool PAIRS, typename K>
-__device__ __noinline__ bool bucket_sort_chunk(const TileChunk &C, K *keys, uint32_t *vals,
-                                               const Offsets &off, K *tmp_keys,
-                                               uint32_t *tmp_vals, unsigned char *smem,
-                                               uint32_t *hb, int *warp_s);
-
-// Shortest average segment of a chunk the bucket sort is tried on: below it
-// the comparison sort is faster (its merge levels stop at the segment length;
-// on GB300, 2^24 u32 pairs: 0.20 against 0.25 ms at 64 keys per segment, even
-// at 128).
-constexpr int64_t kBucketMinAvg = 128;
 
 // ---------------------------------------------------------------------------
 // One CTA of the tile sort: tile t of a problem whose half-tile map is
 // half_first (null: the problem is one tile).  With tmp_keys given the CTA
 // also forms the CAP-runs of the long segments of at most radix_min
-// elements (plan_tile).  kBucket: chunks of segments of kBucketMinAvg keys
-// or more on average try the bucket sort first.
+// elements (plan_tile).
 // ---------------------------------------------------------------------------
-template <typename K, bool PAIRS, int NT, int KPT, bool kBucket = false>
+template <typename K, bool PAIRS, int NT, int KPT>
 __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restrict__ vals,
                                          const Offsets &off, const int32_t *__restrict__ half_first,
                                          int64_t t, K *__restrict__ tmp_keys = nullptr,
@@ -878,14 +863,9 @@ __device__ __forceinline__ void tile_cta(K *__restrict__ keys, uint32_t *__restr
     plan_tile<Cfg::CAP>(off, half_first, t, tmp_keys != nullptr, radix_min, plan_s);
   __syncthreads();
   const int nc = plan_s.nc;
-  for (int c = 0; c < nc; ++c) {
-    const TileChunk &C = plan_s.c[c];
-    if (kBucket && static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg <= C.m &&
-        bucket_sort_chunk<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s))
-      continue;
+  for (int c = 0; c < nc; ++c)
     sort_tile_chunk<Cfg, PAIRS>(plan_s.c[c], keys, vals, off, tmp_keys, tmp_vals, smem, hb,
                                 warp_s);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -900,25 +880,4 @@ tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                               radix_min);
 }
 
-// ---------------------------------------------------------------------------
-// Batched form: the tiles of every instance of a batch in one launch.  CTA t
-// belongs to the last instance whose first tile is at or before t and sorts
-// that instance's local tile; each instance has its own half-tile map, so a
-// CTA never mixes instances.
-// ---------------------------------------------------------------------------
-template <typename K, bool PAIRS, int NT, int KPT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-tile_sort_batch_kernel(const BatchInst *__restrict__ tab, int32_t count,
-                       const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
-                       uint32_t *__restrict__ tmp_vals, int64_t radix_min) {
-  const int64_t t = blockIdx.x;
-  const int32_t i = find_instance(tab, count, t, &BatchInst::tile_base);
-  const BatchInst &I = tab[i];
-  tile_cta<K, PAIRS, NT, KPT, true>(static_cast<K *>(I.keys), I.vals, I.offsets_view(),
-                              half_first + I.half_base, t - I.tile_base, tmp_keys + I.tmp_base,
-                              PAIRS ? tmp_vals + I.tmp_base : nullptr, radix_min);
-}
-
 }  // namespace segsort
-
-#include "bucket_sort.cuh"
