@@ -296,20 +296,28 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
   const int sh = leading_zeros(varying);
   const int seg_sh = one_flag & kSegShared;
   // ---- bucket of every key; count (the old count is the key's slot) ----------------
+  // The key's scaled position in its segment: bucket s + floor(x * len / 2^W)
+  // and, in frac, the rest x * len mod 2^W (where it lies inside that bucket).
+  auto place = [&](int q, int i, Bits &frac) -> int {
+    int s = 0, t = m;
+    if (multi) bounds(i, s, t);
+    const uint32_t len = t > s ? static_cast<uint32_t>(t - s) : 1u;
+    int shift = sh;
+    if (hinted) shift = max(shift, multi ? static_cast<int>(SH[s] & kSegShared) : seg_sh);
+    shift = min(shift, static_cast<int>(8 * sizeof(Bits)) - 1);
+    const Bits x = kb[q] << shift;
+    frac = x * static_cast<Bits>(len);
+    const int b = s + static_cast<int>(bucket_scale<Bits>(x, len));
+    return b < 0 ? 0 : (b >= m ? m - 1 : b);  // only malformed offsets reach the clamp
+  };
   uint32_t pk[IPT];
 #pragma unroll
   for (int q = 0; q < IPT; ++q) {
     const int i = q * NT + tid;
     pk[q] = 0;
     if (i < m) {
-      int s = 0, t = m;
-      if (multi) bounds(i, s, t);
-      const uint32_t len = t > s ? static_cast<uint32_t>(t - s) : 1u;
-      int shift = sh;
-      if (hinted) shift = max(shift, multi ? static_cast<int>(SH[s] & kSegShared) : seg_sh);
-      shift = min(shift, static_cast<int>(8 * sizeof(Bits)) - 1);
-      int b = s + static_cast<int>(bucket_scale<Bits>(kb[q] << shift, len));
-      b = b < 0 ? 0 : (b >= m ? m - 1 : b);  // only malformed offsets reach the clamp
+      Bits frac;
+      const int b = place(q, i, frac);
       const uint32_t slot = atomicAdd(&CN[BL::cslot(b)], 1u);
       pk[q] = static_cast<uint32_t>(b) | (slot << 16);
     }
@@ -317,7 +325,7 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
   __syncthreads();
   // ---- exclusive scan of the counts (thread t: buckets [t*IPT, t*IPT+IPT));
   // sum of squared sizes and the largest bucket -------------------------------------
-  {
+  auto scan_counts = [&](uint32_t &sq_all, uint32_t &mx_all) {
     uint32_t sum = 0, sq = 0, mx = 0;
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
@@ -342,17 +350,57 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       red_s[0][warp] = sq_w;
       red_s[1][warp] = mx_w;
     }
-  }
-  __syncthreads();
-  uint32_t sq_all = 0, mx_all = 0;
+    __syncthreads();
+    sq_all = 0;
+    mx_all = 0;
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    sq_all += red_s[0][w];
-    mx_all = max(mx_all, red_s[1][w]);
-  }
-  if (sq_all > kBucketSkew * static_cast<uint32_t>(m) || mx_all > kBucketMaxSize) {
-    if (from_tmp) write_back(false);
-    return false;
+    for (int w = 0; w < NW; ++w) {
+      sq_all += red_s[0][w];
+      mx_all = max(mx_all, red_s[1][w]);
+    }
+  };
+  auto skewed = [&](uint32_t sq_all, uint32_t mx_all) {
+    return sq_all > kBucketSkew * static_cast<uint32_t>(m) || mx_all > kBucketMaxSize;
+  };
+  uint32_t sq_all, mx_all;
+  scan_counts(sq_all, mx_all);
+  if (skewed(sq_all, mx_all)) {
+    // Second level: the keys of bucket c (start S, n keys) spread over the n
+    // positions [S, S + n) by where they lie inside c (frac), which evens out
+    // densities that vary over the key range (float bit patterns, for one:
+    // every binade is a quarter of the patterns of the one above it but may
+    // hold more keys).  Still in key order: a finer bucket of c is one of
+    // c's positions, and frac grows with the key inside c.
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+      if (q * NT + tid < m) {
+        const int c = static_cast<int>(pk[q] & 0xFFFFu);
+        const uint32_t S = CN[BL::cslot(c)];
+        pk[q] = S | ((CN[BL::cslot(c + 1)] - S) << 16);
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < BL::kCntSlots; i += NT) CN[i] = 0u;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+      const int i = q * NT + tid;
+      if (i < m) {
+        Bits frac;
+        place(q, i, frac);
+        const uint32_t S = pk[q] & 0xFFFFu, n = max(pk[q] >> 16, 1u);
+        int f = static_cast<int>(S + bucket_scale<Bits>(frac, n));
+        f = f >= m ? m - 1 : f;
+        const uint32_t slot = atomicAdd(&CN[BL::cslot(f)], 1u);
+        pk[q] = static_cast<uint32_t>(f) | (slot << 16);
+      }
+    }
+    __syncthreads();
+    scan_counts(sq_all, mx_all);
+    if (skewed(sq_all, mx_all)) {
+      if (from_tmp) write_back(false);
+      return false;
+    }
   }
   // ---- scatter to the buckets --------------------------------------------------------
 #pragma unroll
