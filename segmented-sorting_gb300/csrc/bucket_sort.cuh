@@ -270,16 +270,17 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       }
     }
   };
-  Bits all_and = ~Bits(0), all_or = 0;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    Bits a = red_s[0][w], o = red_s[2][w];
+  // The warps' partials, combined across the lanes of every warp.
+  static_assert(NW <= 32, "the warp partials fit one warp");
+  Bits all_and, all_or;
+  {
+    const bool in = lane < NW;
+    all_and = __reduce_and_sync(0xFFFFFFFFu, in ? red_s[0][lane] : 0xFFFFFFFFu);
+    all_or = __reduce_or_sync(0xFFFFFFFFu, in ? red_s[2][lane] : 0u);
     if constexpr (sizeof(Bits) == 8) {
-      a |= static_cast<Bits>(red_s[1][w]) << 32;
-      o |= static_cast<Bits>(red_s[3][w]) << 32;
+      all_and |= static_cast<Bits>(__reduce_and_sync(0xFFFFFFFFu, in ? red_s[1][lane] : 0xFFFFFFFFu)) << 32;
+      all_or |= static_cast<Bits>(__reduce_or_sync(0xFFFFFFFFu, in ? red_s[3][lane] : 0u)) << 32;
     }
-    all_and &= a;
-    all_or |= o;
   }
   const Bits varying = all_and ^ all_or;  // bits that are not the same in every key
   if (varying == 0) {
@@ -351,13 +352,8 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       red_s[1][warp] = mx_w;
     }
     __syncthreads();
-    sq_all = 0;
-    mx_all = 0;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      sq_all += red_s[0][w];
-      mx_all = max(mx_all, red_s[1][w]);
-    }
+    sq_all = __reduce_add_sync(0xFFFFFFFFu, lane < NW ? red_s[0][lane] : 0u);
+    mx_all = __reduce_max_sync(0xFFFFFFFFu, lane < NW ? red_s[1][lane] : 0u);
   };
   auto skewed = [&](uint32_t sq_all, uint32_t mx_all) {
     return sq_all > kBucketSkew * static_cast<uint32_t>(m) || mx_all > kBucketMaxSize;

@@ -397,16 +397,19 @@ __device__ __forceinline__ uint32_t block_exclusive_add(uint32_t v, uint32_t &to
   }
   if (lane == 31) warp_s[warp] = static_cast<int>(x);
   __syncthreads();
-  uint32_t before = 0, all = 0;
+  // Every warp scans the warp totals across its lanes.
+  constexpr int NW = NT / 32;
+  static_assert(NW <= 32, "the warp totals fit one warp");
+  uint32_t w = lane < NW ? static_cast<uint32_t>(warp_s[lane]) : 0u;
 #pragma unroll
-  for (int w = 0; w < NT / 32; ++w) {
-    const uint32_t ws = static_cast<uint32_t>(warp_s[w]);
-    before += w < warp ? ws : 0u;
-    all += ws;
+  for (int o = 1; o < NW; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+    if (lane >= o) w += y;
   }
+  const uint32_t before = __shfl_sync(0xFFFFFFFFu, w, warp > 0 ? warp - 1 : 0);
+  total = __shfl_sync(0xFFFFFFFFu, w, NW - 1);
   __syncthreads();
-  total = all;
-  return before + x - v;
+  return (warp > 0 ? before : 0u) + x - v;
 }
 
 // Writes a sorted chunk: thread t holds the words of positions
