@@ -405,13 +405,16 @@ int segsort_get_param(int param, int64_t *value);
  * segsort_tune_pairs_u32 sorts the given problem like segsort_pairs_u32, but
  * first measures it -- on copies of the inputs, each route timed three times
  * after one untimed call -- under candidate routes: the radix threshold
- * (4096, 2^15, 2^17, off), the streamed-tile kernel (never, always) and the
- * long-segment kernel's resident CTAs per SM (1, 2, all), one after the
- * other, keeping a candidate that is at least 2% faster.  The chosen route is
- * returned (optional outputs), recorded for the problem's class in this
- * process, and appended to cache_path (optional) as a line
- *   plain k<key bytes> n<log2 n> len<log2 (n / nseg)> <radix> <stream> <ctas>
- * Later plain calls of that class (any key type of the same width) take the
+ * (4096, 2^15, 2^17, off), the streamed-tile kernel (never, always), the
+ * long-segment kernel's resident CTAs per SM (1, 2, all), the bucket-route
+ * threshold (off, 64, 256) and the MSD route (the other setting), one after
+ * the other, keeping a candidate that is at least 2% faster.  The chosen
+ * route is returned (optional outputs: its first three fields), recorded for
+ * the problem's class in this process, and appended to cache_path (optional)
+ * as a line
+ *   plain k<key bytes> n<log2 n> len<log2 (n / nseg)> <radix> <stream> <ctas> <bucket> <msd>
+ * (a line without the last two fields loads them at their defaults, 128 and
+ * 1).  Later plain calls of that class (any key type of the same width) take the
  * recorded route.  segsort_tune_load reads such lines from a file into the
  * process's table (returns how many, or SEGSORT_ERR_INVALID_ARG when the
  * file cannot be read; lines of other formats are skipped);

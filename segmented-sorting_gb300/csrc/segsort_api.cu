@@ -94,7 +94,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // MSD route (msd_route.cuh): problems whose average segment is longer than
   // the radix threshold, in a workspace the library owns (the expansion's
   // arrays grow with nseg).
-  const bool msd = g_msd_on.load(std::memory_order_relaxed) != 0 && ws == nullptr &&
+  const bool msd = R.msd != 0 && ws == nullptr &&
                    n > std::max<int64_t>(L.radix_min, R.radix_min) * static_cast<int64_t>(nseg);
   const int64_t c_len = msd ? msd_stage2_segments(nseg, L.max_rjobs) : 0;
   size_t msd_at[6] = {0, 0, 0, 0, 0, 0};  // sub, flags, jbeg, jidx, jextra, end
@@ -200,7 +200,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // offsets with empty segments, so n / O.nseg understates them).
     const bool short_avg =
         !msd && R.stream_max_avg > 0 && n <= R.stream_max_avg * static_cast<int64_t>(nseg);
-    const int64_t bucket_min = g_bucket_min_avg.load(std::memory_order_relaxed);
+    const int64_t bucket_min = R.bucket_min_avg;
     if (short_avg) {
       const unsigned blocks =
           static_cast<unsigned>((W.halves + kClassifyWarps) / kClassifyWarps);  // halves + 1 entries
@@ -378,8 +378,9 @@ int time_route(K *keys, uint32_t *vals, const K *k0, const uint32_t *v0, int64_t
 }
 
 // Coordinate search over the route of one problem: the radix threshold, then
-// the streamed-tile threshold, then the long-segment kernel's CTAs per SM; a
-// candidate replaces the best so far when it is at least 2% faster.  On
+// the streamed-tile threshold, the long-segment kernel's CTAs per SM, the
+// bucket-route threshold and the MSD route; a candidate replaces the best so
+// far when it is at least 2% faster.  On
 // return the caller's buffers hold the problem sorted with the chosen route.
 template <typename K, bool PAIRS>
 int tune_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_t nseg,
@@ -437,6 +438,17 @@ int tune_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   for (int32_t v : {1, 2}) {
     CallRoute R = *best;
     R.merge_per_sm = v;
+    consider(R);
+  }
+  const auto bucket_on = [&](int64_t v) { return v > 0 && n >= v * static_cast<int64_t>(nseg); };
+  for (int64_t v : {int64_t{0}, int64_t{64}, int64_t{256}}) {  // bucket route: off, wider, narrower
+    CallRoute R = *best;
+    R.bucket_min_avg = v;
+    if (bucket_on(v) != bucket_on(start.bucket_min_avg)) consider(R);
+  }
+  if (n > best->radix_min * static_cast<int64_t>(nseg)) {  // MSD route: the other choice
+    CallRoute R = *best;
+    R.msd = best->msd ? 0 : 1;
     consider(R);
   }
   // The caller's buffers end sorted with the chosen route.
@@ -639,9 +651,10 @@ int segsort_tune_pairs_u32(uint32_t *k, uint32_t *v, int64_t n, const int32_t *o
     record_route(cls, R);
     if (cache_path != nullptr) {
       if (FILE *f = std::fopen(cache_path, "a")) {
-        std::fprintf(f, "plain k%u n%u len%u %lld %lld %d\n", cls >> 16, (cls >> 8) & 255u, cls & 255u,
-                     static_cast<long long>(R.radix_min), static_cast<long long>(R.stream_max_avg),
-                     R.merge_per_sm);
+        std::fprintf(f, "plain k%u n%u len%u %lld %lld %d %lld %d\n", cls >> 16, (cls >> 8) & 255u,
+                     cls & 255u, static_cast<long long>(R.radix_min),
+                     static_cast<long long>(R.stream_max_avg), R.merge_per_sm,
+                     static_cast<long long>(R.bucket_min_avg), R.msd);
         std::fclose(f);
       }
     }
@@ -661,15 +674,17 @@ int segsort_tune_load(const char *cache_path) {
   int loaded = 0;
   while (std::fgets(line, sizeof(line), f)) {
     unsigned kb = 0, lgn = 0, lgl = 0;
-    long long radix = 0, stream = 0;
-    int merge = 0;
-    if (std::sscanf(line, "plain k%u n%u len%u %lld %lld %d", &kb, &lgn, &lgl, &radix, &stream,
-                    &merge) != 6)
-      continue;  // another tuner's line
+    long long radix = 0, stream = 0, bucket = 128;
+    int merge = 0, msd = 1;
+    // Lines of six fields (written before the bucket and MSD fields existed)
+    // take those two at their defaults.
+    const int got = std::sscanf(line, "plain k%u n%u len%u %lld %lld %d %lld %d", &kb, &lgn, &lgl,
+                                &radix, &stream, &merge, &bucket, &msd);
+    if (got != 6 && got != 8) continue;  // another tuner's line
     if ((kb != 4 && kb != 8) || lgn > 40 || lgl > 40 || radix < 0 || stream < 0 || merge < 0 ||
-        merge > 64)
+        merge > 64 || bucket < 0 || (msd != 0 && msd != 1))
       continue;
-    record_route((kb << 16) | (lgn << 8) | lgl, CallRoute{radix, stream, merge});
+    record_route((kb << 16) | (lgn << 8) | lgl, CallRoute{radix, stream, merge, bucket, msd});
     ++loaded;
   }
   std::fclose(f);

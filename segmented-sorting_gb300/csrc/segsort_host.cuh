@@ -109,14 +109,17 @@ inline std::atomic<int64_t> g_bucket_min_avg{128};
 inline std::atomic<int64_t> g_msd_on{1};
 
 // ---------------------------------------------------------------------------
-// Route of one plain call: the radix threshold, the streamed-tile threshold
-// and the resident CTAs per SM of the long-segment kernel (0: as many as
-// fit).  From the process-wide parameters, unless the tuner recorded a route
-// for the call's class (segsort_tune_pairs_u32 / segsort_tune_load).
+// Route of one plain call: the radix threshold, the streamed-tile threshold,
+// the resident CTAs per SM of the long-segment kernel (0: as many as fit),
+// the bucket-route threshold and the MSD route switch.  From the process-wide
+// parameters, unless the tuner recorded a route for the call's class
+// (segsort_tune_pairs_u32 / segsort_tune_load).
 struct CallRoute {
   int64_t radix_min;
   int64_t stream_max_avg;
   int32_t merge_per_sm;
+  int64_t bucket_min_avg = 128;  // bucket route from this average segment on (0: never)
+  int32_t msd = 1;               // MSD route for calls whose segments average above radix_min
 };
 
 // Class of a plain call: key width, log2 of n, log2 of the average segment.
@@ -151,7 +154,9 @@ inline bool tuned_route(uint32_t cls, CallRoute *r) {
 
 template <typename K>
 inline CallRoute route_for(int64_t n, int32_t nseg) {
-  CallRoute r{radix_min_for<K>(), g_stream_max_avg.load(std::memory_order_relaxed), 0};
+  CallRoute r{radix_min_for<K>(), g_stream_max_avg.load(std::memory_order_relaxed), 0,
+              g_bucket_min_avg.load(std::memory_order_relaxed),
+              static_cast<int32_t>(g_msd_on.load(std::memory_order_relaxed))};
   CallRoute t;
   if (tuned_route(route_class(static_cast<int>(sizeof(K)), n, nseg), &t)) {
     r = t;

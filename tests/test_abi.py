@@ -231,8 +231,9 @@ def test_tuned_route_table(pkg, tmp_path):
     cache = tmp_path / "routes.txt"
     cache.write_text("t1-n24-max20-len10 3\n"             # a batch-plan line
                      "plain k4 n24 len10 32768 32 2\n"
-                     "plain k8 n20 len4 4096 0 0\n"
+                     "plain k8 n20 len4 4096 0 0 64 0\n"  # with the bucket and MSD fields
                      "plain k4 n24 len10 131072 0 1\n"     # a later line wins
+                     "plain k4 n22 len10 131072 0 1 128 2\n"  # MSD field out of range
                      "garbage\n")
     L.segsort_tune_clear()
     r, st, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()

@@ -36,7 +36,7 @@ def test_tuner_sorts_records_and_routes(pkg, cuda, oracle, inst, tmp_path):
     ek, ev = oracle.segsort_numpy(keys, off, vals)
     assert np.array_equal(dk.cpu().numpy().view(np.uint32), ek)
     assert np.array_equal(dv.cpu().numpy().view(np.uint32), ev)
-    assert r.value in (4096, 1 << 15, 1 << 17, 1 << 30)
+    assert r.value in (4096, 1 << 15, 1 << 17, 1 << 30, pkg.get_param(pkg.PARAM_RADIX_MIN_32))
     assert c.value in (0, 1, 2)
     assert cache.read_text().startswith("plain k4 n20 len")
     # recorded for this process ...
