@@ -295,6 +295,17 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     return false;
   }
   const int sh = leading_zeros(varying);
+  // Fewer possible key values than half the keys of an average segment
+  // (low-entropy keys): equal keys would fill the buckets whatever the
+  // scaling, and their atomics would serialise.  Refused before counting.
+  {
+    const int span = static_cast<int>(8 * sizeof(Bits)) - sh;  // bits that can differ
+    const int64_t avg = m / max(C.hi - C.lo, 1);
+    if (span < 31 && (int64_t{1} << span) < avg / 2) {
+      if (from_tmp) write_back(false);
+      return false;
+    }
+  }
   const int seg_sh = one_flag & kSegShared;
   // ---- bucket of every key; count (the old count is the key's slot) ----------------
   // The key's scaled position in its segment: bucket s + floor(x * len / 2^W)
@@ -499,13 +510,22 @@ template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_list_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                  K *__restrict__ tmp_keys, uint32_t *__restrict__ tmp_vals,
-                 const TileChunk *__restrict__ list, const uint32_t *count, int64_t max_list) {
+                 const TileChunk *__restrict__ list, const uint32_t *count, int64_t max_list,
+                 uint32_t *tickets) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t hb[Cfg::CAP / 32];
   __shared__ int warp_s[NT / 16];
+  __shared__ int64_t next_s;
   const int64_t c = min(static_cast<int64_t>(*count), max_list);
-  for (int64_t i = blockIdx.x; i < c; i += gridDim.x) {
+  // Chunks are taken from a ticket counter: a static split over the
+  // resident CTAs ends unevenly (chunks cost alike).
+  for (;;) {
+    if (threadIdx.x == 0) next_s = static_cast<int64_t>(atomicAdd(tickets, 1u));
+    __syncthreads();
+    const int64_t i = next_s;
+    __syncthreads();
+    if (i >= c) break;
     const TileChunk C = list[i];
     sort_tile_chunk<Cfg, PAIRS>(C, keys, vals, off, tmp_keys, tmp_vals, smem, hb, warp_s);
   }
@@ -534,13 +554,19 @@ template <typename K, bool PAIRS, int NT, int KPT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 tile_list_batch_kernel(const BatchInst *__restrict__ tab, K *__restrict__ tmp_keys,
                        uint32_t *__restrict__ tmp_vals, const TileChunk *__restrict__ list,
-                       const uint32_t *count, int64_t max_list) {
+                       const uint32_t *count, int64_t max_list, uint32_t *tickets) {
   using Cfg = TileConfig<K, PAIRS, NT, KPT>;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t hb[Cfg::CAP / 32];
   __shared__ int warp_s[NT / 16];
+  __shared__ int64_t next_s;
   const int64_t c = min(static_cast<int64_t>(*count), max_list);
-  for (int64_t i = blockIdx.x; i < c; i += gridDim.x) {
+  for (;;) {
+    if (threadIdx.x == 0) next_s = static_cast<int64_t>(atomicAdd(tickets, 1u));
+    __syncthreads();
+    const int64_t i = next_s;
+    __syncthreads();
+    if (i >= c) break;
     const TileChunk C = list[i];
     const BatchInst &I = tab[C.inst];
     sort_tile_chunk<Cfg, PAIRS>(C, static_cast<K *>(I.keys), I.vals, I.offsets_view(),

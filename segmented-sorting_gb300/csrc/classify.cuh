@@ -29,6 +29,7 @@ enum : int {
   kCtrRTiles = 9,     // radix tiles of all radix jobs
   kCtrRDigits = 10,   // OR over radix jobs of their digits that vary
   kCtrFallback = 11,  // tile chunks the bucket sort left to the comparison sort
+  kCtrListTicket = 12,  // next listed chunk a comparison-sort CTA takes
   kCtrWords = 16,
 };
 

@@ -257,7 +257,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, tiles));
       list_kernel<<<lgrid, Cfg::NT, Cfg::kSmemBytes, stream>>>(
           keys, vals, O, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
-          W.max_fallback);
+          W.max_fallback, W.ctr + kCtrListTicket);
       rec.tile_launches = 2;
     } else {
       tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(

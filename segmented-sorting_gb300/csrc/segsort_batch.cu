@@ -195,7 +195,8 @@ struct BatchKernels {
     const unsigned lgrid =
         static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S.sms, G.tiles));
     list<<<lgrid, TCfg::NT, TCfg::kSmemBytes, stream>>>(tab, W.tmp_keys, W.tmp_vals, W.fallback,
-                                                      W.ctr + kCtrFallback, W.max_fallback);
+                                                      W.ctr + kCtrFallback, W.max_fallback,
+                                                      W.ctr + kCtrListTicket);
     if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
     const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     const int64_t items = G.total_n / MergeShape<K>::T + 1;
