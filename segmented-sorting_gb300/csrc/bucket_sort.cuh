@@ -165,6 +165,7 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     for (int i = tid; i < HW; i += NT) hb[i] = 0u;
   // ---- segment heads; per head word the last head before it and the first
   // after it ------------------------------------------------------------------------
+  bool other_buffer = false;  // a segment whose keys are not where the speculative load read
   if (multi) {
     __syncthreads();  // cleared head words
     for (int64_t j = C.lo + tid; j < C.hi; j += NT) {
@@ -172,10 +173,14 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       const int64_t p = b0 - C.a;
       if (p >= 0 && p < m) {
         atomicOr(&hb[p >> 5], 1u << (p & 31));
-        if (hinted && off(j + 1) > b0) SH[p] = off.flags[j];
+        if (hinted && off(j + 1) > b0) {
+          const uint8_t f = off.flags[j];
+          SH[p] = f;
+          other_buffer |= ((f & kSegTmp) != 0) != spec_tmp;
+        }
       }
     }
-    __syncthreads();
+    other_buffer = __syncthreads_or(other_buffer);
     if (warp == 0) {
       int last[WPL], first[WPL];
       int lmax = -1, lmin = m;
@@ -214,7 +219,7 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     }
     __syncthreads();
   }
-  if (hinted && multi) {
+  if (other_buffer) {
 #pragma unroll
     for (int q = 0; q < IPT; ++q) {
       const int i = q * NT + tid;
