@@ -174,13 +174,22 @@ int launch_batch(segsort_server_s *S, const std::vector<Request *> &rs, BatchRec
   if (cudaEventRecord(S->ev_in, S->s_in) != cudaSuccess ||
       cudaStreamWaitEvent(S->s_sort, S->ev_in, 0) != cudaSuccess)
     return fail(SEGSORT_ERR_CUDA);
-  const int rc = segsort_pairs_batch(items.data(), static_cast<int32_t>(items.size()), S->s_sort);
+  // A batch of one request is a plain call (the same kernels without the
+  // batch's table upload and per-group launches; at low load most batches
+  // hold one request).
+  const int rc =
+      items.size() == 1
+          ? segsort_pairs_u32(static_cast<uint32_t *>(items[0].d_keys), items[0].d_vals,
+                              items[0].n, items[0].d_offsets, items[0].nseg, S->s_sort)
+          : segsort_pairs_batch(items.data(), static_cast<int32_t>(items.size()), S->s_sort);
   if (rc != SEGSORT_OK) return fail(rc);
-  if (cudaLaunchHostFunc(S->s_sort, on_sorted, S) != cudaSuccess) return fail(SEGSORT_ERR_CUDA);
-  *sorted_cb = true;
+  // The copies out wait for the sort, not for the host callback after it
+  // (a host function holds its stream until it returns).
   if (cudaEventRecord(S->ev_sorted, S->s_sort) != cudaSuccess ||
       cudaStreamWaitEvent(S->s_out, S->ev_sorted, 0) != cudaSuccess)
     return fail(SEGSORT_ERR_CUDA);
+  if (cudaLaunchHostFunc(S->s_sort, on_sorted, S) != cudaSuccess) return fail(SEGSORT_ERR_CUDA);
+  *sorted_cb = true;
   for (size_t i = 0; i < rs.size(); ++i) {
     const Request &r = *rs[i];
     const size_t kb = static_cast<size_t>(r.n) * 4;
