@@ -630,14 +630,15 @@ def run_ours(args) -> None:
                 out.append(d)
         return out
 
-    def msd_oversize_keys(lg: int, d: int) -> int:
-        """Keys in sub-buckets (segment, value of digit d) longer than a tile:
-        the MSD route's second stage gives them one merge pass (sub-buckets
-        are at most two tiles long)."""
+    def msd_oversize_bytes(lg: int, d: int) -> int:
+        """Merge-pass bytes of the sub-buckets (segment, value of digit d)
+        longer than a tile: the MSD route's second stage gives each of them
+        merge_passes(length) passes (sub-buckets are at most four tiles)."""
         k = pristine[lg].long() & 0xFFFFFFFF
         sub = ((torch.arange(n, device=dev) >> lg) << 8) | ((k >> (8 * d)) & 255)
         c = torch.bincount(sub, minlength=(n >> lg) << 8)
-        return int(c[c > cap].sum())
+        big = c[c > cap].tolist()
+        return sum(BYTES_PER_PAIR * x * merge_passes(x) for x in big)
 
     # Algorithmic bytes per launch.  The tile kernels read and write every
     # key and value once and read the offsets: all of them when the segments
@@ -671,8 +672,7 @@ def run_ours(args) -> None:
             digits = varying_digits(lg)
             if msd_on and len(digits) >= 3:
                 bucket_bytes[lg] = BYTES_PER_PAIR * n
-                long_bytes[lg] = (4 * n + BYTES_PER_PAIR * n
-                                  + BYTES_PER_PAIR * msd_oversize_keys(lg, digits[-1]))
+                long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n + msd_oversize_bytes(lg, digits[-1])
             else:
                 idle_tile.append(lg)  # the tile kernel finds no work: every segment is on the radix route
                 passes = len(digits)

@@ -66,6 +66,8 @@ struct LargeWs {
   // passes; the long-segment kernel then returns before the merge passes.
   int32_t msd_stage;
   int32_t tile_cap;       // keys per tile of the tile sort
+  int64_t lsd_min;        // MSD stage: a segment that does not qualify and is not longer than
+                          // this is left to the second stage's merge passes
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {

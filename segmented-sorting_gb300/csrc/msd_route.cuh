@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(256) msd_expand_kernel(Offsets off, LargeWs<K>
     }
     const int64_t base = j + M.jextra[lo];
     if (lo < nj && M.jbeg[lo] == s && e - s > ws.radix_min) {
-      if (!(ws.rdigits[M.jidx[lo]] & kRDigitMsd)) put(base, s, kSegSkip);  // stage 1 finished it
+      const uint32_t v = ws.rdigits[M.jidx[lo]];
+      if (!(v & kRDigitMsd))  // stage 1 finished it, or left it to the second stage
+        put(base, s, (v & kRDigitDefer) ? 0 : kSegSkip);
     } else {
       put(base, s, 0);
     }

@@ -73,13 +73,17 @@ constexpr int kLookEagerSpins = 32;      // polls before the look-back backs off
 // mask bits alone.
 constexpr uint32_t kRDigitMsd = 1u << 16;
 constexpr uint32_t kRDigitMask = kRDigitMsd - 1u;
+// rdigits flag of a segment the MSD stage leaves unsorted (it does not
+// qualify and is not longer than the LSD threshold): the second stage sorts
+// it like any other segment.
+constexpr uint32_t kRDigitDefer = 1u << 17;
 // A segment takes the MSD route when at least this many digit positions vary
 // (fewer LSD passes cost less than the MSD pass, its copy-back and the tile
 // pass over the sub-buckets) ...
 constexpr int kMsdMinDigits = 3;
 // ... and no bucket of its top varying digit holds more than this many keys
 // times the tile capacity (a larger sub-bucket takes the merge passes).
-constexpr int kMsdMaxBucketTiles = 2;
+constexpr int kMsdMaxBucketTiles = 4;
 
 template <typename K, bool PAIRS, int NT>
 struct RadixShape {
@@ -455,6 +459,8 @@ __device__ __forceinline__ void radix_phases(const Space &sp, const LargeWs<K> &
       const int64_t lim = min(static_cast<int64_t>(kMsdMaxBucketTiles) * ws.tile_cap, ws.radix_min);
       if (mx <= static_cast<uint64_t>(lim)) varying = (1u << dt) | kRDigitMsd;
     }
+    if (ws.msd_stage && !(varying & kRDigitMsd) && static_cast<int64_t>(len) <= ws.lsd_min)
+      varying = kRDigitDefer;
     if (tid == 0) {
       ws.rdigits[j] = varying;
       if (varying) atomicOr(&ws.ctr[kCtrRDigits], varying);

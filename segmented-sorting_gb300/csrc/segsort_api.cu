@@ -89,13 +89,14 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
   // ---- workspace ----------------------------------------------------------------
   // A caller's workspace is sized for every radix threshold
   // (segsort_workspace_bytes); the library's own is sized for the current one.
-  const WsLayout L =
-      ws != nullptr ? layout_any_threshold<K, PAIRS>(n) : layout_for<K, PAIRS>(n, R.radix_min);
   // MSD route (msd_route.cuh): problems whose average segment is longer than
-  // the radix threshold, in a workspace the library owns (the expansion's
-  // arrays grow with nseg).
-  const bool msd = R.msd != 0 && ws == nullptr &&
-                   n > std::max<int64_t>(L.radix_min, R.radix_min) * static_cast<int64_t>(nseg);
+  // the MSD threshold, in a workspace the library owns (the expansion's
+  // arrays grow with nseg).  Its first stage takes the segments longer than
+  // that threshold, which may be below the radix threshold.
+  const int64_t msd_min = msd_min_for<K>(R.radix_min);
+  const bool msd = R.msd != 0 && ws == nullptr && n > msd_min * static_cast<int64_t>(nseg);
+  const WsLayout L = ws != nullptr ? layout_any_threshold<K, PAIRS>(n)
+                                   : layout_for<K, PAIRS>(n, msd ? msd_min : R.radix_min);
   const int64_t c_len = msd ? msd_stage2_segments(nseg, L.max_rjobs) : 0;
   size_t msd_at[6] = {0, 0, 0, 0, 0, 0};  // sub, flags, jbeg, jidx, jextra, end
   if (msd) {
@@ -127,6 +128,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
 
   LargeWs<K> W = ws_views<K, PAIRS>(base, L);
   W.radix_min = std::max<int64_t>(L.radix_min, R.radix_min);
+  W.lsd_min = W.radix_min;
 
   // The long-segment kernel: radix passes, then merge passes, one cooperative
   // launch (returns at once without long segments).  All resident CTAs, but
@@ -171,6 +173,8 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
         rc = SEGSORT_ERR_CUDA;
         break;
       }
+      const int64_t lsd_radix_min = W.radix_min;
+      W.radix_min = std::max<int64_t>(msd_min, L.radix_min);  // stage 1's jobs
       segment_classify(off);
       if (prof) rec.m0 = prof_event(stream);
       W.msd_stage = 1;
@@ -187,6 +191,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
         break;
       }
       O = Offsets{M.sub, static_cast<int32_t>(c_len), 0, n, M.flags};
+      W.radix_min = lsd_radix_min;
     }
     // ---- classify: half-tile -> first segment map, jobs for long segments ----
     if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess) {

@@ -89,6 +89,19 @@ inline int64_t radix_min_for() {
       (sizeof(K) == 8 ? g_radix_min64 : g_radix_min32).load(std::memory_order_relaxed));
 }
 
+// Segments longer than this try the MSD route (in calls that take it) even
+// below the radix threshold; one that does not qualify and is not longer
+// than the radix threshold goes back to the merge passes.  Measured on GB300
+// (2^24 pairs, 64-bit keys whose top varying digit splits them finely): the
+// MSD route 0.77 / 0.73 / 0.82 ms at 2^15 / 2^16 / 2^17 against the merge
+// route's 0.88 / 1.05 / 1.21 ms; for 32-bit keys it meets the merge route at
+// 2^16, the radix threshold.
+template <typename K>
+inline int64_t msd_min_for(int64_t radix_min) {
+  const int64_t m = sizeof(K) == 8 ? (int64_t{1} << 15) : (int64_t{1} << 16);
+  return clamp_radix_min<K>(std::min(radix_min, m));
+}
+
 // Problems whose average segment is at most this long take the half-tile
 // classify and the streamed tile kernel (measured on GB300 over 2^24 pairs:
 // both faster up to 32, slower from 64).  Run-time parameter
@@ -277,6 +290,7 @@ inline LargeWs<K> ws_views(unsigned char *base, const WsLayout &L) {
   W.max_rtiles = L.max_rtiles;
   W.radix_min = L.radix_min;
   W.msd_stage = 0;
+  W.lsd_min = L.radix_min;
   W.tile_cap = static_cast<int32_t>(tile_cap<K>());
   return W;
 }
