@@ -90,3 +90,25 @@ def test_cfg2_lengths_full_size(pkg, cuda, inst):
         torch.cuda.synchronize()
         assert pkg.device_status() == 0
         assert_stable_sorted(torch, before, _u32_bits(dk), dv.long(), off)
+
+
+@pytest.mark.parametrize("kind", ["full_range", "two_digits", "narrow_top", "one_value"])
+def test_u64_below_the_radix_threshold(pkg, cuda, oracle, inst, kind):
+    """64-bit keys at the default thresholds: the MSD route takes segments
+    above 2^15 although the radix threshold is 2^18; a segment that does not
+    qualify (fewer than three varying digits, or a top digit that leaves long
+    sub-buckets) is left to the merge passes of the second stage."""
+    length = 40000
+    n = 4 * length + 1234
+    off = np.concatenate([inst.equal_offsets(4 * length, length), [n]]).astype(np.int32)
+    keys = inst.uniform_keys(n, seed=77, bits=64, dtype=np.uint64)
+    if kind == "two_digits":
+        keys &= np.uint64(0xFFFF)
+    elif kind == "narrow_top":
+        # four varying digits, but the top one takes two values: sub-buckets
+        # of about 20000 keys, longer than four tiles
+        keys = ((keys >> np.uint64(63)) << np.uint64(56)) | (keys & np.uint64(0xFFFFFF))
+    elif kind == "one_value":
+        keys[:] = np.uint64(0x0123456789ABCDEF)
+    with pkg.params({pkg.PARAM_MSD: 1}):
+        check_both(pkg, cuda, oracle, keys, off)
