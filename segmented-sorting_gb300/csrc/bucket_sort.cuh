@@ -85,9 +85,10 @@ struct BucketLayout {
 
 // Sorts chunk C by buckets, or returns false (uniformly over the CTA) having
 // written nothing.  Every thread of the CTA calls it; hb is the tile
-// kernel's head bitmask (CAP / 32 words), warp_s its scan scratch.  Starts and
-// ends with a barrier, so it may follow and precede any other use of the
-// shared memory.
+// kernel's head bitmask (CAP / 32 words), warp_s its scan scratch.  It passes
+// a barrier before its first shared-memory write, so it may follow any other
+// use of the shared memory; the caller synchronises before using the shared
+// memory after it (the next call does).
 template <typename Cfg, bool PAIRS, typename K>
 __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, uint32_t *vals,
                                                  const Offsets &off, K *tmp_keys,
@@ -291,7 +292,6 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
   if (varying == 0) {
     // Every key is equal: the stable order is the input order.
     if (from_tmp || C.tmp) write_back(C.tmp != 0);
-    __syncthreads();
     return true;
   }
   if (hinted && static_cast<int64_t>(C.hi - C.lo) * kBucketMinAvg > m) {
@@ -352,7 +352,7 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       mx = max(mx, c);
     }
     uint32_t total;
-    uint32_t run = block_exclusive_add<NT>(sum, total, warp_s);
+    uint32_t run = block_exclusive_add<NT, false>(sum, total, warp_s);  // barrier below
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
       uint32_t *at = CN + BL::cslot(tid * IPT + j);
@@ -451,7 +451,6 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
     io.dst_keys[S + r] = Ord::from_bits(WT::bits(w));
     if constexpr (PAIRS) io.dst_vals[S + r] = SV[p];
   }
-  __syncthreads();
   return true;
 }
 

@@ -386,7 +386,9 @@ __device__ __forceinline__ void block_exmax_max(int a, int b, int &a_before, int
 }
 
 // Block-wide sum (exclusive prefix and total) of one value per thread.
-template <int NT>
+// kSyncAfter: a closing barrier, so that warp_s may be written again at
+// once (callers that pass another barrier first leave it out).
+template <int NT, bool kSyncAfter = true>
 __device__ __forceinline__ uint32_t block_exclusive_add(uint32_t v, uint32_t &total, int *warp_s) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
@@ -408,7 +410,7 @@ __device__ __forceinline__ uint32_t block_exclusive_add(uint32_t v, uint32_t &to
   }
   const uint32_t before = __shfl_sync(0xFFFFFFFFu, w, warp > 0 ? warp - 1 : 0);
   total = __shfl_sync(0xFFFFFFFFu, w, NW - 1);
-  __syncthreads();
+  if constexpr (kSyncAfter) __syncthreads();
   return (warp > 0 ? before : 0u) + x - v;
 }
 
