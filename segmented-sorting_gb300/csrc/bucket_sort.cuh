@@ -72,8 +72,11 @@ __device__ __forceinline__ int leading_zeros<uint64_t>(uint64_t x) {
 template <typename Cfg, bool PAIRS>
 struct BucketLayout {
   static constexpr int CAP = Cfg::CAP;
-  static constexpr size_t kWords = 0;                                        // Word[CAP]
-  static constexpr size_t kVals = kWords + CAP * sizeof(typename Cfg::Word);  // uint32[CAP]
+  // Word[CAP + kPad]: the words past the chunk's last read as the largest
+  // word, so the ranking of a bucket near the end never compares garbage.
+  static constexpr int kPad = 8;
+  static constexpr size_t kWords = 0;
+  static constexpr size_t kVals = kWords + (CAP + kPad) * sizeof(typename Cfg::Word);  // uint32[CAP]
   static constexpr size_t kBkt = kVals + (PAIRS ? CAP * sizeof(uint32_t) : 0);  // uint16[CAP]
   static constexpr size_t kCnt = (kBkt + CAP * sizeof(uint16_t) + 15) / 16 * 16;
   // Bucket counters, then starts: one padding word per 32 keeps the blocked
@@ -426,6 +429,7 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       SB[p] = static_cast<uint16_t>(b);
     }
   }
+  if (tid < BL::kPad) SW[m + tid] = WT::maxv();
   __syncthreads();
   // ---- every slot's key to its place: its bucket's start plus the bucket's
   // words below it ----------------------------------------------------------------
@@ -440,12 +444,17 @@ __device__ __forceinline__ bool bucket_sort_body(const TileChunk &C, K *keys, ui
       for (int y = S; y < E; ++y) r += WT::lt(SW[y], w);
     } else if (n > 1) {
       // Fixed trip count: a warp whose buckets differ in size does not
-      // diverge.  Words past E (other buckets, or not written) are read but
-      // not counted; y stays inside the array.
+      // diverge.  Words past E are read (at most kBucketUnroll - 2 of them,
+      // inside the padded array).  In a chunk of one segment they are never
+      // below w -- later buckets hold larger keys, the padding the largest
+      // word -- so they need no test; with several segments the next
+      // segment's first buckets may hold smaller keys, so they are masked.
+      if (!multi) {
 #pragma unroll
-      for (int k = 0; k < kBucketUnroll; ++k) {
-        const int y = min(S + k, CAP - 1);
-        r += (k < n) & WT::lt(SW[y], w);
+        for (int k = 0; k < kBucketUnroll; ++k) r += WT::lt(SW[S + k], w);
+      } else {
+#pragma unroll
+        for (int k = 0; k < kBucketUnroll; ++k) r += (k < n) & WT::lt(SW[S + k], w);
       }
     }
     io.dst_keys[S + r] = Ord::from_bits(WT::bits(w));
