@@ -18,11 +18,16 @@
 // on consecutive positions.
 //
 // The ranking costs the sum of the squared bucket sizes.  When that sum is
-// above kBucketSkew * m, or a bucket holds more than kBucketMaxSize keys (few
-// distinct keys, skewed keys, keys of a segment packed in a narrow range),
-// the function writes nothing and returns false, and the caller sorts the
-// chunk with the comparison sort.  A chunk whose keys are all equal is
-// already in its stable order (copied when the result goes elsewhere).
+// above kBucketSkew * m, or a bucket holds more than kBucketMaxSize keys, a
+// second level spreads every bucket's keys over the bucket's own positions by
+// where they lie inside it (x * (t - s) mod 2^W), which evens out densities
+// that vary over the key range (float bit patterns).  A chunk still skewed
+// after that (few distinct keys, many equal keys), or one whose keys can take
+// fewer values than half its average segment, is refused: the function
+// returns false having written nothing to the result (a chunk read from the
+// temporary buffers is first copied to the caller's), and the caller sorts
+// it with the comparison sort.  A chunk whose keys are all equal is already
+// in its stable order (copied when the result goes elsewhere).
 //
 // The result is the same as the comparison sort's, bit for bit: both give the
 // stable order of each segment, which is unique.  The reference sorts these
