@@ -126,11 +126,15 @@ __device__ __forceinline__ void classify_boundary(const Offsets &off, int64_t s,
   }
 }
 
-// Appends one long segment to the merge or the radix job list.
+// Appends long segment seg (from beg to end) to the merge or the radix job
+// list; nothing for a segment its flags mark as already sorted.
 template <typename K>
-__device__ __forceinline__ void add_long_job(const LargeWs<K> &ws, int64_t beg, int64_t end,
+__device__ __forceinline__ void add_long_job(const LargeWs<K> &ws, const Offsets &off,
+                                             int64_t seg, int64_t beg, int64_t end,
                                              int32_t inst) {
-  const int4 job = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end), 0, inst);
+  if (off.flags != nullptr && (off.flags[seg] & kSegSkip)) return;
+  const int4 job = make_int4(static_cast<int32_t>(beg), static_cast<int32_t>(end),
+                             static_cast<int32_t>(seg), inst);
   const bool radix = end - beg > ws.radix_min;
   const uint32_t j = atomicAdd(&ws.ctr[radix ? kCtrRJobs : kCtrJobs], 1u);
   if (j < static_cast<uint32_t>(radix ? ws.max_rjobs : ws.max_jobs))
@@ -203,7 +207,7 @@ large_classify_halves_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> 
     const int64_t a = lb_s[w], b = lb_s[w + 1];
     if (b > a) {
       const int64_t beg = off(b - 1), end = off(b);
-      if (end - beg > cap) add_long_job(ws, beg, end, 0);
+      if (end - beg > cap) add_long_job(ws, off, b - 1, beg, end, 0);
     }
   }
 }
@@ -238,7 +242,7 @@ large_classify_halves_batch_kernel(const BatchInst *__restrict__ tab, int32_t co
     if (b > a) {
       const Offsets off = tab[i].offsets_view();
       const int64_t beg = off(b - 1), end = off(b);
-      if (end - beg > cap) add_long_job(ws, beg, end, i);
+      if (end - beg > cap) add_long_job(ws, off, b - 1, beg, end, i);
     }
   }
 }

@@ -140,4 +140,123 @@ __global__ void __launch_bounds__(kRBuckets) msd_sub_kernel(LargeWs<K> ws, MsdWs
   }
 }
 
+// ---------------------------------------------------------------------------
+// The batched form: one expansion per key-type group.  Jobs carry their
+// instance (int4 .w) and segment (.z); every instance has its own
+// second-stage offsets and flags (the stage-2 table's offsets / flags, its
+// nseg the padded count c_len) and owns the expansion entries
+// [msd_base, msd_base + c_len + 1) of the flat thread index.
+struct MsdBatchWs {
+  int32_t *jbeg;    // [max_rjobs] radix job begins, by (instance, begin)
+  int32_t *jidx;    // [max_rjobs] the job of each
+  int32_t *jinst;   // [max_rjobs] its instance
+  int32_t *jextra;  // [max_rjobs] entries the instance's MSD jobs before it add (255 each)
+};
+
+// Thread per radix job q: its rank by (instance, begin) and the MSD jobs of
+// its instance before it.
+template <typename K>
+__global__ void __launch_bounds__(256) msd_rank_batch_kernel(LargeWs<K> ws, MsdBatchWs M) {
+  const int32_t nj = min(static_cast<int32_t>(ld_volatile(&ws.ctr[kCtrRJobs])), ws.max_rjobs);
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= nj) return;
+  const int4 me = ws.rjobs[q];
+  int32_t rank = 0, msd_before = 0;
+  for (int32_t r = 0; r < nj; ++r) {
+    const int32_t w = __ldg(&ws.rjobs[r].w), x = __ldg(&ws.rjobs[r].x);
+    if (w < me.w || (w == me.w && x < me.x)) {
+      ++rank;
+      if (w == me.w) msd_before += (__ldg(&ws.rdigits[r]) & kRDigitMsd) != 0u;
+    }
+  }
+  if (rank >= nj) return;  // only with malformed (overlapping) offsets
+  M.jbeg[rank] = me.x;
+  M.jidx[rank] = static_cast<int32_t>(q);
+  M.jinst[rank] = me.w;
+  M.jextra[rank] = (kRBuckets - 1) * msd_before;
+}
+
+// First rank in [lo, hi) whose (instance, begin) is at or above (w, x).
+__device__ __forceinline__ int32_t msd_lower_bound(const MsdBatchWs &M, int32_t lo, int32_t hi,
+                                                   int32_t w, int64_t x) {
+  while (lo < hi) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (M.jinst[mid] < w || (M.jinst[mid] == w && M.jbeg[mid] < x)) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Thread per expansion entry: entry j < nseg of an instance is its segment j
+// (one entry, at j plus the extra entries of the instance's MSD jobs before
+// it; an MSD segment's 256 are msd_sub_batch_kernel's); the entries from
+// nseg on fill the instance's padding with n.
+template <typename K>
+__global__ void __launch_bounds__(256)
+msd_expand_batch_kernel(const BatchInst *__restrict__ tab1, const BatchInst *__restrict__ tab2,
+                        int32_t count, int64_t entries, LargeWs<K> ws, MsdBatchWs M) {
+  const int32_t nj = min(static_cast<int32_t>(ld_volatile(&ws.ctr[kCtrRJobs])), ws.max_rjobs);
+  const int64_t f = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (f >= entries) return;
+  const int32_t i = find_instance(tab2, count, f, &BatchInst::msd_base);
+  const BatchInst &I2 = tab2[i];
+  const Offsets off = tab1[i].offsets_view();
+  int32_t *sub = const_cast<int32_t *>(I2.offsets);
+  uint8_t *flags = const_cast<uint8_t *>(I2.flags);
+  const int64_t c_len = I2.nseg;
+  const int64_t j = f - I2.msd_base;
+  // The instance's jobs and the extra entries of all of its MSD jobs.
+  const int32_t r0 = msd_lower_bound(M, 0, nj, i, INT64_MIN);
+  const int32_t r1 = msd_lower_bound(M, r0, nj, i + 1, INT64_MIN);
+  const int64_t all_extra =
+      r1 > r0 ? M.jextra[r1 - 1] + (kRBuckets - 1) * ((ws.rdigits[M.jidx[r1 - 1]] & kRDigitMsd) != 0u)
+              : 0;
+  auto put = [&](int64_t at, int64_t v, uint8_t sk) {
+    if (at >= 0 && at < c_len) {
+      sub[at] = static_cast<int32_t>(v);
+      flags[at] = sk;
+    }
+  };
+  if (j < off.nseg) {
+    const int64_t s = off(j), e = off(j + 1);
+    const int32_t lo = msd_lower_bound(M, r0, r1, i, s);
+    const int64_t base = j + (lo < r1 ? M.jextra[lo] : all_extra);
+    if (lo < r1 && M.jbeg[lo] == s && e - s > ws.radix_min) {
+      const uint32_t v = ws.rdigits[M.jidx[lo]];
+      if (!(v & kRDigitMsd)) put(base, s, (v & kRDigitDefer) ? 0 : kSegSkip);
+    } else {
+      put(base, s, 0);
+    }
+  } else {
+    const int64_t at = off.nseg + all_extra + (j - off.nseg);
+    if (at <= c_len) {
+      if (at < c_len) flags[at] = 0;
+      if (at >= 0) sub[at] = static_cast<int32_t>(off.n);
+    }
+  }
+}
+
+// Block per radix job (by rank), thread per bucket g: entry g of an MSD
+// segment in its instance's second-stage offsets.
+template <typename K>
+__global__ void __launch_bounds__(kRBuckets)
+msd_sub_batch_kernel(const BatchInst *__restrict__ tab2, LargeWs<K> ws, MsdBatchWs M) {
+  constexpr int64_t D = sizeof(typename KeyOrder<K>::Bits);
+  const int32_t nj = min(static_cast<int32_t>(ld_volatile(&ws.ctr[kCtrRJobs])), ws.max_rjobs);
+  const int32_t r = blockIdx.x;
+  if (r >= nj) return;
+  const int32_t q = M.jidx[r];
+  const uint32_t v = ws.rdigits[q];
+  if (!(v & kRDigitMsd)) return;
+  const int4 jb = ws.rjobs[q];
+  const BatchInst &I2 = tab2[jb.w];
+  const int dt = 31 - __clz(v & kRDigitMask);
+  const int g = threadIdx.x;
+  const int64_t at = static_cast<int64_t>(jb.z) + M.jextra[r] + g;
+  const uint32_t st = ws.rhist[(static_cast<int64_t>(q) * D + dt) * kRBuckets + g];
+  if (at >= 0 && at < I2.nseg) {
+    const_cast<int32_t *>(I2.offsets)[at] = jb.x + static_cast<int32_t>(st);
+    const_cast<uint8_t *>(I2.flags)[at] = static_cast<uint8_t>(8 * (D - dt)) | kSegTmp;
+  }
+}
+
 }  // namespace segsort

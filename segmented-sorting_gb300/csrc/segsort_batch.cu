@@ -43,7 +43,28 @@ struct Group {
   WsLayout L;
   size_t tab_off = 0;  // table position in the batch buffer
   size_t ws_off = 0;   // workspace position in the batch buffer
+  // MSD route (msd_route.cuh): its stage-2 table and the expansion's arrays.
+  bool msd = false;
+  int64_t lsd_min = 0;        // the radix threshold of stage 2
+  int64_t msd_entries = 0;    // expansion entries: sum over instances of c_len + 1
+  std::vector<int64_t> c_len; // per instance: its padded stage-2 segment count
+  size_t tab2_off = 0, sub_off = 0, flags_off = 0, rank_off = 0;
 };
+
+// The stage-2 table of an MSD group: every instance with its expanded
+// offsets and flags (pointers into the batch buffer at buf).
+std::vector<BatchInst> stage2_table(const Group &G, unsigned char *buf) {
+  std::vector<BatchInst> t = G.insts;
+  int32_t *sub = reinterpret_cast<int32_t *>(buf + G.sub_off);
+  uint8_t *flags = reinterpret_cast<uint8_t *>(buf + G.flags_off);
+  for (size_t i = 0; i < t.size(); ++i) {
+    t[i].offsets = sub + t[i].msd_base;
+    t[i].flags = flags + t[i].msd_base;
+    t[i].nseg = static_cast<int32_t>(G.c_len[i]);
+    t[i].heads = 0;
+  }
+  return t;
+}
 
 struct BatchLayout {
   std::vector<Group> groups;
@@ -62,6 +83,11 @@ int64_t item_of(int type) {
 
 int64_t radix_min_of(int type) {
   return type == SEGSORT_KEY_U64 ? radix_min_for<uint64_t>() : radix_min_for<uint32_t>();
+}
+
+int64_t msd_min_of(int type) {
+  return type == SEGSORT_KEY_U64 ? msd_min_for<uint64_t>(radix_min_for<uint64_t>())
+                                 : msd_min_for<uint32_t>(radix_min_for<uint32_t>());
 }
 
 // Validates the items and lays out every group.  Empty items (n == 0 or
@@ -98,15 +124,43 @@ int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B)
     if (G.total_n > kGroupMaxN) return SEGSORT_ERR_TOO_LARGE;
   }
   size_t off = 0;
+  const bool msd_on = g_msd_on.load(std::memory_order_relaxed) != 0;
   for (int t = 0; t < kKeyTypes; ++t) {
     Group &G = g[t];
     if (G.insts.empty()) continue;
+    // The MSD route for a group of 64-bit keys when an instance may hold a
+    // segment above its threshold.  (Measured on the 64-instance benchmark
+    // batch: the u64 group 3.13 -> 2.59 ms; the u32 and f32 groups, whose
+    // long segments take four LSD passes, 1.38 -> 1.55 and 2.00 -> 2.18 ms,
+    // the second stage's classify and expansion over all their instances
+    // costing more than the passes saved.)
+    const int64_t msd_min = msd_min_of(t);
+    G.lsd_min = radix_min_of(t);
+    if (key_bytes_of(t) == 8)
+      for (const BatchInst &I : G.insts) G.msd = G.msd || (msd_on && I.n > msd_min);
     G.L = make_layout(G.total_n, key_bytes_of(t), 4, cap_of(t), item_of(t), G.half_entries,
-                      radix_min_of(t));
+                      G.msd ? std::min(msd_min, G.lsd_min) : G.lsd_min);
     G.tab_off = off;
     off = align256(off + G.insts.size() * sizeof(BatchInst));
     G.ws_off = off;
     off = align256(off + G.L.total);
+    if (G.msd) {
+      for (BatchInst &I : G.insts) {
+        const int64_t c = msd_stage2_segments(I.nseg, I.n / (msd_min + 1) + 1);
+        if (c >= (int64_t{1} << 31)) return SEGSORT_ERR_TOO_LARGE;
+        I.msd_base = G.msd_entries;
+        G.c_len.push_back(c);
+        G.msd_entries += c + 1;
+      }
+      G.tab2_off = off;
+      off = align256(off + G.insts.size() * sizeof(BatchInst));
+      G.sub_off = off;
+      off = align256(off + static_cast<size_t>(G.msd_entries) * 4);
+      G.flags_off = off;
+      off = align256(off + static_cast<size_t>(G.msd_entries));
+      G.rank_off = off;
+      off = align256(off + 4 * (static_cast<size_t>(G.L.max_rjobs) + 1) * 4);
+    }
     B.groups.push_back(std::move(G));
   }
   B.total = off;
@@ -117,7 +171,7 @@ int build_layout(const segsort_batch_item *items, int32_t count, BatchLayout &B)
 // Table upload without host synchronisation: the entries travel as kernel
 // parameters (one launch per block of kUploadBlock entries), so the host
 // array may be freed as soon as the launch returns.
-constexpr int kUploadBlock = 48;  // 48 * 72 bytes: inside the 4 KB parameter space
+constexpr int kUploadBlock = 44;  // 44 * 88 bytes: inside the 4 KB parameter space
 struct UploadBlock {
   BatchInst v[kUploadBlock];
   int32_t count;
@@ -174,47 +228,78 @@ struct BatchKernels {
   static int enqueue(const Group &G, unsigned char *buf, const DeviceState &S, int dev,
                      cudaStream_t stream, int merge_per_sm) {
     const BatchInst *tab = reinterpret_cast<const BatchInst *>(buf + G.tab_off);
+    // The tables stage 2 reads: the expanded offsets of an MSD group.
+    const BatchInst *tab2 =
+        G.msd ? reinterpret_cast<const BatchInst *>(buf + G.tab2_off) : tab;
     const int32_t count = static_cast<int32_t>(G.insts.size());
-    const LargeWs<K> W = ws_views<K, true>(buf + G.ws_off, G.L);
+    LargeWs<K> W = ws_views<K, true>(buf + G.ws_off, G.L);
+    W.lsd_min = G.lsd_min;
     const int64_t cap = tile_cap<K>();
-    if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess)
-      return SEGSORT_ERR_CUDA;
     const unsigned cls_blocks =
         static_cast<unsigned>((G.half_entries + kClassifyWarps - 1) / kClassifyWarps);
-    classify<<<cls_blocks, (kClassifyWarps + 1) * 32, 0, stream>>>(tab, count, G.half_entries, cap,
-                                                                   cap / 2, W);
-    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
-
-    // Tile sort first: it forms the sorted runs the merge passes read (the
-    // radix passes read the caller's buffers, which it leaves alone).
-    bucket<<<static_cast<unsigned>(G.tiles), BCfg::NT, kBSmem, stream>>>(
-        tab, count, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min, W.fallback,
-        W.ctr + kCtrFallback, W.max_fallback);
-    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
-    const int lo = occupancy(list, TCfg::NT, TCfg::kSmemBytes, list_occ, dev);
-    const unsigned lgrid =
-        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S.sms, G.tiles));
-    list<<<lgrid, TCfg::NT, TCfg::kSmemBytes, stream>>>(tab, W.tmp_keys, W.tmp_vals, W.fallback,
-                                                      W.ctr + kCtrFallback, W.max_fallback,
-                                                      W.ctr + kCtrListTicket);
-    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    auto classify_on = [&](const BatchInst *t, const LargeWs<K> &w) {
+      if (cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), stream) != cudaSuccess)
+        return false;
+      classify<<<cls_blocks, (kClassifyWarps + 1) * 32, 0, stream>>>(t, count, G.half_entries,
+                                                                     cap, cap / 2, w);
+      return cudaGetLastError() == cudaSuccess;
+    };
     const int mo = occupancy(merge, kMThreads, MS::kBytes, merge_occ, dev);
     const int64_t items = G.total_n / MergeShape<K>::T + 1;
     const int per_sm = merge_per_sm > 0 ? std::min(merge_per_sm, mo) : mo;
     const unsigned grid =
         static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(per_sm) * S.sms, items));
-    BatchSpace<K> sp{tab, W.tmp_keys, W.tmp_vals};
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kMThreads);
-    cfg.dynamicSmemBytes = MS::kBytes;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (cudaLaunchKernelEx(&cfg, merge, sp, W, cap) != cudaSuccess) return SEGSORT_ERR_CUDA;
+    auto launch_long = [&](const BatchInst *t, LargeWs<K> w) {
+      BatchSpace<K> sp{t, W.tmp_keys, W.tmp_vals};
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grid);
+      cfg.blockDim = dim3(kMThreads);
+      cfg.dynamicSmemBytes = MS::kBytes;
+      cfg.stream = stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      return cudaLaunchKernelEx(&cfg, merge, sp, w, cap) == cudaSuccess;
+    };
+
+    if (G.msd) {
+      // ---- MSD route, stage 1: the radix segments above the MSD threshold
+      // (one pass on the top varying digit, or all their LSD passes, or none
+      // for those left to stage 2), then the expanded offsets -------------------
+      LargeWs<K> W1 = W;  // radix_min: the layout's, the MSD threshold
+      W1.msd_stage = 1;
+      if (!classify_on(tab, W1) || !launch_long(tab, W1)) return SEGSORT_ERR_CUDA;
+      const size_t rj = static_cast<size_t>(G.L.max_rjobs) + 1;
+      int32_t *rk = reinterpret_cast<int32_t *>(buf + G.rank_off);
+      MsdBatchWs M{rk, rk + rj, rk + 2 * rj, rk + 3 * rj};
+      msd_rank_batch_kernel<K><<<static_cast<unsigned>((G.L.max_rjobs + 255) / 256), 256, 0,
+                                 stream>>>(W1, M);
+      msd_expand_batch_kernel<K><<<static_cast<unsigned>((G.msd_entries + 255) / 256), 256, 0,
+                                   stream>>>(tab, tab2, count, G.msd_entries, W1, M);
+      msd_sub_batch_kernel<K><<<static_cast<unsigned>(G.L.max_rjobs), kRBuckets, 0, stream>>>(
+          tab2, W1, M);
+      if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    }
+    LargeWs<K> W2 = W;
+    W2.radix_min = std::max<int64_t>(G.lsd_min, W.radix_min);
+    if (!classify_on(tab2, W2)) return SEGSORT_ERR_CUDA;
+
+    // Tile sort first: it forms the sorted runs the merge passes read (the
+    // radix passes read the caller's buffers, which it leaves alone).
+    bucket<<<static_cast<unsigned>(G.tiles), BCfg::NT, kBSmem, stream>>>(
+        tab2, count, W2.half_first, W2.tmp_keys, W2.tmp_vals, W2.radix_min, W2.fallback,
+        W2.ctr + kCtrFallback, W2.max_fallback);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    const int lo = occupancy(list, TCfg::NT, TCfg::kSmemBytes, list_occ, dev);
+    const unsigned lgrid =
+        static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S.sms, G.tiles));
+    list<<<lgrid, TCfg::NT, TCfg::kSmemBytes, stream>>>(tab2, W2.tmp_keys, W2.tmp_vals,
+                                                      W2.fallback, W2.ctr + kCtrFallback,
+                                                      W2.max_fallback, W2.ctr + kCtrListTicket);
+    if (cudaGetLastError() != cudaSuccess) return SEGSORT_ERR_CUDA;
+    if (!launch_long(tab2, W2)) return SEGSORT_ERR_CUDA;
     return SEGSORT_OK;
   }
 };
@@ -333,7 +418,9 @@ int segsort_pairs_batch(const segsort_batch_item *items, int32_t count, segsort_
   }
   for (const Group &G : B.groups) {
     if (upload_table(G.insts, reinterpret_cast<BatchInst *>(buf + G.tab_off), stream) !=
-        cudaSuccess) {
+            cudaSuccess ||
+        (G.msd && upload_table(stage2_table(G, buf), reinterpret_cast<BatchInst *>(buf + G.tab2_off),
+                               stream) != cudaSuccess)) {
       rc = SEGSORT_ERR_CUDA;
       break;
     }
@@ -373,6 +460,14 @@ int segsort_batch_plan_create(const segsort_batch_item *items, int32_t count,
                      cudaMemcpyHostToDevice) != cudaSuccess) {
         rc = SEGSORT_ERR_CUDA;
         break;
+      }
+      if (G.msd) {
+        const std::vector<BatchInst> t2 = stage2_table(G, buf);
+        if (cudaMemcpy(buf + G.tab2_off, t2.data(), t2.size() * sizeof(BatchInst),
+                       cudaMemcpyHostToDevice) != cudaSuccess) {
+          rc = SEGSORT_ERR_CUDA;
+          break;
+        }
       }
     }
     if (rc != SEGSORT_OK) break;

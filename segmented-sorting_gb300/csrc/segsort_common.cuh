@@ -96,14 +96,18 @@ struct BatchInst {
   void *keys;
   uint32_t *vals;
   const int32_t *offsets;
+  const uint8_t *flags;  // per-segment flags (Offsets::flags) or null
   int64_t n;
   int64_t tmp_base;
   int64_t half_base;
   int64_t tile_base;
+  int64_t msd_base;      // the instance's first entry in the MSD route's expansion
   int32_t nseg;
   int32_t heads;
 
-  __device__ __forceinline__ Offsets offsets_view() const { return Offsets{offsets, nseg, heads, n}; }
+  __device__ __forceinline__ Offsets offsets_view() const {
+    return Offsets{offsets, nseg, heads, n, flags};
+  }
 };
 
 // The last instance whose `field` is at or below x (instances with equal

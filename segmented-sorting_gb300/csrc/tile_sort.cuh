@@ -727,7 +727,7 @@ constexpr int kMaxTileChunks = 5;
 struct TileChunk {
   int64_t a;
   int32_t lo, hi, m, tmp;
-  int32_t inst = 0;  // instance of a batch (the bucket route's fallback list)
+  int32_t inst;  // instance of a batch (the bucket route's fallback list; 0 otherwise)
 };
 struct TilePlan {
   TileChunk c[kMaxTileChunks];

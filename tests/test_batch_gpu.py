@@ -105,12 +105,16 @@ def _oracle_of(oracle, keys, off, heads):
     return oracle.segsort_numpy(keys, csr, np.arange(len(keys), dtype=np.uint32))
 
 
-def test_batch_mix_matches_oracle_and_plain(pkg, cuda, inst, oracle):
+@pytest.mark.parametrize("msd", [1, 0], ids=["msd_route", "lsd_route"])
+def test_batch_mix_matches_oracle_and_plain(pkg, cuda, inst, oracle, msd):
+    """With the MSD route on, the 64-bit key group (instances above 2^15
+    keys) runs its two stages (per-instance expanded offsets)."""
     torch = cuda
     dev = [_DevInstance(torch, k, np.arange(len(k), dtype=np.uint32), o, t, h)
            for k, o, t, h in _mix(inst)]
     items = (pkg.BatchItem * len(dev))(*[d.item(pkg) for d in dev])
-    rc = pkg.lib().segsort_pairs_batch(items, len(dev), torch.cuda.current_stream().cuda_stream)
+    with pkg.params({pkg.PARAM_MSD: msd}):
+        rc = pkg.lib().segsort_pairs_batch(items, len(dev), torch.cuda.current_stream().cuda_stream)
     assert rc == pkg.SEGSORT_OK
     torch.cuda.synchronize()
     assert pkg.device_status() == pkg.SEGSORT_OK
