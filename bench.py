@@ -606,6 +606,7 @@ def run_ours(args) -> None:
     stream_max_avg = pkg.get_param(pkg.PARAM_STREAM_MAX_AVG)
     bucket_min_avg = pkg.get_param(pkg.PARAM_BUCKET_MIN_AVG)
     msd_on = pkg.get_param(pkg.PARAM_MSD)
+    tiny_max_avg = pkg.get_param(pkg.PARAM_TINY_MAX_AVG)
     launches_per_step = sum(p["tile_launches"] + p["large_launches"] for p in phase.values())
 
     def merge_passes(length: int) -> int:
@@ -651,17 +652,21 @@ def run_ours(args) -> None:
     # threshold whose keys vary in at least three digits) reads every key for
     # the counts and every pair once in its one pass (long-segment kernel),
     # then every pair once in the bucket kernel, plus a merge pass over the
-    # sub-buckets longer than a tile.  The library runs the streamed tile
-    # kernel when the average segment is at most stream_max_avg long, the
-    # bucket route (tile_bucket_kernel, and tile_list_kernel for the chunks it
+    # sub-buckets longer than a tile.  The library runs the tiny route
+    # (tile_tiny_kernel, and tile_list_kernel for the chunks it lists) when
+    # the average segment is at most tiny_max_avg long, the streamed tile
+    # kernel when it is at most stream_max_avg long, the bucket route (tile_bucket_kernel, and tile_list_kernel for the chunks it
     # refuses) from bucket_min_avg on, the one-CTA-per-tile comparison sort
     # between.
     tile_bytes, stream_bytes, bucket_bytes, long_bytes, idle_tile = {}, {}, {}, {}, []
+    tiny_bytes = {}
     for lg in lengths:
         ln = 1 << lg
         full = BYTES_PER_PAIR * n + 4 * (n // ln + 1)
         tile_table = bucket_bytes if bucket_min_avg and ln >= bucket_min_avg else tile_bytes
-        if ln <= stream_max_avg:
+        if ln <= stream_max_avg and ln <= tiny_max_avg:
+            tiny_bytes[lg] = full
+        elif ln <= stream_max_avg:
             stream_bytes[lg] = full
         elif ln <= cap:
             tile_table[lg] = full
@@ -679,6 +684,7 @@ def run_ours(args) -> None:
                 long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n * (passes + (passes & 1))
     kernels = {}
     for name, table, key in (("tile_sort_kernel", tile_bytes, "tile_ms"),
+                             ("tile_tiny_kernel", tiny_bytes, "tile_ms"),
                              ("tile_stream_kernel", stream_bytes, "tile_ms"),
                              ("tile_bucket_kernel", bucket_bytes, "tile_ms"),
                              ("long_segment_kernel", long_bytes, "large_ms")):
@@ -705,7 +711,7 @@ def run_ours(args) -> None:
                 "traffic_workload": ((tr or {}).get(name) or {}).get("workload"),
                 "radix_min": radix_min, "stream_max_avg": stream_max_avg,
                 "bucket_min_avg": bucket_min_avg, "msd": msd_on,
-                "kernels": kernels}
+                "tiny_max_avg": tiny_max_avg, "kernels": kernels}
 
     # ---- end to end through the public API with host buffers ---------------
     e2e = None

@@ -390,6 +390,10 @@ int segsort_pool_bytes(int *created, uint64_t *used);
  *     workspace, sorts its radix segments whose keys vary in at least three
  *     8-bit digits by one radix pass on the top varying digit and then the
  *     tile sort of the 256 sub-buckets, instead of one pass per digit.
+ *   SEGSORT_PARAM_TINY_MAX_AVG: problems whose average segment is at most this
+ *     long (and at most the streamed-tile threshold) take the tiny route: a
+ *     rank sort of chunks of segments of at most 8 keys, the comparison sort
+ *     for the other chunks; 0 turns it off.
  * A change applies to calls made after it; batch plans keep the values they
  * were created with.  SEGSORT_ERR_INVALID_ARG for an unknown parameter or a
  * value out of range. */
@@ -398,6 +402,7 @@ int segsort_pool_bytes(int *created, uint64_t *used);
 #define SEGSORT_PARAM_STREAM_MAX_AVG 3
 #define SEGSORT_PARAM_BUCKET_MIN_AVG 4
 #define SEGSORT_PARAM_MSD 5
+#define SEGSORT_PARAM_TINY_MAX_AVG 6
 int segsort_set_param(int param, int64_t value);
 int segsort_get_param(int param, int64_t *value);
 

@@ -36,6 +36,7 @@ PARAM_RADIX_MIN_64 = 2
 PARAM_STREAM_MAX_AVG = 3
 PARAM_BUCKET_MIN_AVG = 4
 PARAM_MSD = 5
+PARAM_TINY_MAX_AVG = 6
 
 KEY_TYPES = ("u32", "i32", "f32", "u64")
 KEY_TYPE_CODES = {"u32": 0, "i32": 1, "f32": 2, "u64": 3}  # SEGSORT_KEY_* of include/segsort.h

@@ -222,7 +222,37 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     // sort dominates, and the hardware scheduler balances the tiles better
     // than a static split over resident CTAs.
     if (prof) rec.t0 = prof_event(stream);
-    if (short_avg) {
+    const int64_t tiny_max = g_tiny_max_avg.load(std::memory_order_relaxed);
+    const bool tiny = short_avg && tiny_max > 0 && n <= tiny_max * static_cast<int64_t>(nseg);
+    if (tiny) {
+      // Tiny route: the rank sort of chunks of segments of at most kTinyMax
+      // keys, two tiles' copies in flight per CTA; the other chunks listed
+      // for the comparison sort.
+      using TL = TinyLayout<K, PAIRS, Cfg::CAP>;
+      auto tiny_kernel = tile_tiny_kernel<K, PAIRS, kTinyThreads, Cfg::CAP, 2>;
+      auto list_kernel =
+          tile_list_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
+      static std::atomic<uint64_t> tiny_attr_done{0}, tlist_attr_done{0};
+      static std::atomic<int> tiny_occ[kMaxDevices], tlist_occ[kMaxDevices];
+      if (ensure_smem(tiny_kernel, TL::kBytes, tiny_attr_done, dev) != cudaSuccess ||
+          ensure_smem(list_kernel, Cfg::kSmemBytes, tlist_attr_done, dev) != cudaSuccess) {
+        rc = SEGSORT_ERR_CUDA;
+        break;
+      }
+      const int to = occupancy(tiny_kernel, kTinyThreads, TL::kBytes, tiny_occ, dev);
+      const unsigned tgrid =
+          static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(to) * S->sms, tiles));
+      tiny_kernel<<<tgrid, kTinyThreads, TL::kBytes, stream>>>(
+          keys, vals, O, W.half_first, tiles, true, W.radix_min, W.fallback,
+          W.ctr + kCtrFallback, W.max_fallback);
+      const int lo = occupancy(list_kernel, Cfg::NT, Cfg::kSmemBytes, tlist_occ, dev);
+      const unsigned lgrid =
+          static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, tiles));
+      list_kernel<<<lgrid, Cfg::NT, Cfg::kSmemBytes, stream>>>(
+          keys, vals, O, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
+          W.max_fallback, W.ctr + kCtrListTicket);
+      rec.tile_launches = 2;
+    } else if (short_avg) {
       using SL = StreamLayout<Cfg, K, PAIRS>;
       auto stream_kernel =
           tile_stream_kernel<K, PAIRS, Cfg::NT, Cfg::KPT, TileFor<K, PAIRS>::kMinBlocks>;
@@ -619,6 +649,10 @@ int segsort_set_param(int param, int64_t value) {
       if (value != 0 && value != 1) return SEGSORT_ERR_INVALID_ARG;
       g_msd_on.store(value, std::memory_order_relaxed);
       return SEGSORT_OK;
+    case SEGSORT_PARAM_TINY_MAX_AVG:
+      if (value < 0) return SEGSORT_ERR_INVALID_ARG;
+      g_tiny_max_avg.store(value, std::memory_order_relaxed);
+      return SEGSORT_OK;
     default:
       return SEGSORT_ERR_INVALID_ARG;
   }
@@ -638,6 +672,9 @@ int segsort_get_param(int param, int64_t *value) {
       return SEGSORT_OK;
     case SEGSORT_PARAM_MSD:
       *value = g_msd_on.load(std::memory_order_relaxed);
+      return SEGSORT_OK;
+    case SEGSORT_PARAM_TINY_MAX_AVG:
+      *value = g_tiny_max_avg.load(std::memory_order_relaxed);
       return SEGSORT_OK;
     default:
       return SEGSORT_ERR_INVALID_ARG;

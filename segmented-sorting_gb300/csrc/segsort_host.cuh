@@ -18,6 +18,7 @@
 #include "tile_sort.cuh"
 #include "bucket_sort.cuh"
 #include "tile_stream.cuh"
+#include "tiny_sort.cuh"
 #include "classify.cuh"
 #include "merge_sort.cuh"
 #include "radix_sort.cuh"
@@ -120,6 +121,15 @@ inline std::atomic<int64_t> g_bucket_min_avg{128};
 // the MSD route for their radix segments (msd_route.cuh) when this is set
 // and the library owns the workspace.  Run-time parameter.
 inline std::atomic<int64_t> g_msd_on{1};
+
+// Problems whose average segment is at most this long take the tiny route
+// (tile_tiny_kernel, then tile_list_kernel for the chunks it lists); 0:
+// never.  Run-time parameter.
+inline std::atomic<int64_t> g_tiny_max_avg{8};
+
+// Launch shape of the tiny route: 512 threads, two CTAs per SM (two staging
+// buffers of a tile each).
+constexpr int kTinyThreads = 512;
 
 // ---------------------------------------------------------------------------
 // Route of one plain call: the radix threshold, the streamed-tile threshold,

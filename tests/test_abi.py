@@ -55,16 +55,22 @@ def test_run_time_parameters(pkg):
     """segsort_set_param / segsort_get_param are host-side only."""
     L = pkg.lib()
     saved = {p: pkg.get_param(p) for p in (pkg.PARAM_RADIX_MIN_32, pkg.PARAM_RADIX_MIN_64,
-                                            pkg.PARAM_STREAM_MAX_AVG, pkg.PARAM_BUCKET_MIN_AVG)}
+                                            pkg.PARAM_STREAM_MAX_AVG, pkg.PARAM_BUCKET_MIN_AVG,
+                                            pkg.PARAM_MSD, pkg.PARAM_TINY_MAX_AVG)}
     assert saved[pkg.PARAM_RADIX_MIN_32] >= 4096 and saved[pkg.PARAM_RADIX_MIN_64] >= 4096
     assert saved[pkg.PARAM_BUCKET_MIN_AVG] == 128
+    assert saved[pkg.PARAM_MSD] == 1 and saved[pkg.PARAM_TINY_MAX_AVG] == 8
     with pkg.params({pkg.PARAM_RADIX_MIN_32: 1 << 20, pkg.PARAM_STREAM_MAX_AVG: 0,
-                     pkg.PARAM_BUCKET_MIN_AVG: 0}):
+                     pkg.PARAM_BUCKET_MIN_AVG: 0, pkg.PARAM_MSD: 0, pkg.PARAM_TINY_MAX_AVG: 0}):
         assert pkg.get_param(pkg.PARAM_RADIX_MIN_32) == 1 << 20
         assert pkg.get_param(pkg.PARAM_STREAM_MAX_AVG) == 0
         assert pkg.get_param(pkg.PARAM_BUCKET_MIN_AVG) == 0
+        assert pkg.get_param(pkg.PARAM_MSD) == 0
+        assert pkg.get_param(pkg.PARAM_TINY_MAX_AVG) == 0
     assert {p: pkg.get_param(p) for p in saved} == saved
     assert L.segsort_set_param(pkg.PARAM_BUCKET_MIN_AVG, -5) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_set_param(pkg.PARAM_MSD, 2) == pkg.SEGSORT_ERR_INVALID_ARG
+    assert L.segsort_set_param(pkg.PARAM_TINY_MAX_AVG, -1) == pkg.SEGSORT_ERR_INVALID_ARG
     # below the floor, negative, unknown parameter, missing output
     assert L.segsort_set_param(pkg.PARAM_RADIX_MIN_32, 4095) == pkg.SEGSORT_ERR_INVALID_ARG
     assert L.segsort_set_param(pkg.PARAM_RADIX_MIN_64, 100) == pkg.SEGSORT_ERR_INVALID_ARG
