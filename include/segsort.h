@@ -392,7 +392,7 @@ int segsort_pool_bytes(int *created, uint64_t *used);
  *     tile sort of the 256 sub-buckets, instead of one pass per digit.
  *   SEGSORT_PARAM_TINY_MAX_AVG: problems whose average segment is at most this
  *     long (and at most the streamed-tile threshold) take the tiny route: a
- *     rank sort of chunks of segments of at most 8 keys, the comparison sort
+ *     network sort of chunks of segments of at most 8 keys, the comparison sort
  *     for the other chunks; 0 turns it off.
  * A change applies to calls made after it; batch plans keep the values they
  * were created with.  SEGSORT_ERR_INVALID_ARG for an unknown parameter or a

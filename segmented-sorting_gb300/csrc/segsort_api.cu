@@ -225,7 +225,7 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
     const int64_t tiny_max = g_tiny_max_avg.load(std::memory_order_relaxed);
     const bool tiny = short_avg && tiny_max > 0 && n <= tiny_max * static_cast<int64_t>(nseg);
     if (tiny) {
-      // Tiny route: the rank sort of chunks of segments of at most kTinyMax
+      // Tiny route: the network sort of chunks of segments of at most kTinyMax
       // keys, two tiles' copies in flight per CTA; the other chunks listed
       // for the comparison sort.
       using TL = TinyLayout<K, PAIRS, Cfg::CAP>;

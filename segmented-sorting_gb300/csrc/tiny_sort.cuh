@@ -5,13 +5,14 @@
 // two per SM) take tiles b, b + G, ... and keep two tiles' copies in flight
 // -- the keys, values and segment starts of a tile's first chunk arrive by
 // bulk asynchronous copy into one of two staging buffers, issued two tiles
-// ahead -- and sort a chunk whose segments are all at most kTinyMax keys by
-// ranking in place: every key of segment [s, t) counts the keys of [s, t)
-// below it, and the keys equal to it and before it, which is its place in
-// the stable order, and is written there.  No sort words, no head bitmask,
-// no scan.  A chunk with a longer segment (and any chunk after a tile's
-// first) is appended to the bucket route's fallback list for the comparison
-// sort (tile_list_kernel), CAP-runs of long segments included.
+// ahead.  A chunk whose segments are all at most kTinyMax keys is sorted in
+// the staging buffer, each segment by one thread through a sorting network
+// over (order bits, slot) composites in registers, and goes back to global
+// memory as 16-byte stores (not at all when no key moved: segments of one
+// key, or already in order).  No sort words, no head bitmask, no scan.  A
+// chunk with a longer segment (and any chunk after a tile's first) is
+// appended to the bucket route's fallback list for the comparison sort
+// (tile_list_kernel), CAP-runs of long segments included.
 //
 // The reference sorts these lengths with its smallest bb_segsort bins
 // (register networks of 2..8 keys per thread group, src/bb_segsort/
@@ -23,23 +24,128 @@
 
 namespace segsort {
 
-constexpr int kTinyMax = 8;  // longest segment of a chunk the rank sort takes
+constexpr int kTinyMax = 8;  // longest segment of a chunk the network sort takes
+
+// The keys of one segment of at most kTinyMax keys as (order bits, slot)
+// composites: compared as one value they give the stable order (equal keys
+// by slot), and the slots past the segment hold a composite above every real
+// one, so they sort last whatever the network's width.
+template <typename Bits>
+struct TinyWord;
+template <>
+struct TinyWord<uint32_t> {
+  uint64_t w;  // bits << 4 | slot; the padding ~0
+  __device__ __forceinline__ static TinyWord make(uint32_t bits, int q) {
+    return {(static_cast<uint64_t>(bits) << 4) | static_cast<uint64_t>(q)};
+  }
+  __device__ __forceinline__ static TinyWord pad() { return {~0ull}; }
+  __device__ __forceinline__ uint32_t bits() const { return static_cast<uint32_t>(w >> 4); }
+  __device__ __forceinline__ int slot() const { return static_cast<int>(w & 15u); }
+  __device__ __forceinline__ static void cx(TinyWord &a, TinyWord &b) {
+    const uint64_t lo = min(a.w, b.w), hi = max(a.w, b.w);
+    a.w = lo;
+    b.w = hi;
+  }
+};
+template <>
+struct TinyWord<uint64_t> {
+  uint64_t k;
+  uint32_t q;  // slot; 15 for the padding
+  __device__ __forceinline__ static TinyWord make(uint64_t bits, int q) {
+    return {bits, static_cast<uint32_t>(q)};
+  }
+  __device__ __forceinline__ static TinyWord pad() { return {~0ull, 15u}; }
+  __device__ __forceinline__ uint64_t bits() const { return k; }
+  __device__ __forceinline__ int slot() const { return static_cast<int>(q); }
+  __device__ __forceinline__ static void cx(TinyWord &a, TinyWord &b) {
+    const bool sw = b.k < a.k || (b.k == a.k && b.q < a.q);
+    const TinyWord x = sw ? b : a, y = sw ? a : b;
+    a = x;
+    b = y;
+  }
+};
+
+// Sorts segment [0, len) of the staged keys sk (and values sv), len <= N,
+// in place: composites in N registers through a sorting network of width N
+// -- one comparator for 2 keys, five for 4 (Batcher), nineteen for 8
+// (Batcher's odd-even merge sort; each checked on all 0-1 inputs) -- then
+// every value from its key's original slot.  Returns whether any key moved.
+template <int N, typename K, bool PAIRS>
+__device__ __forceinline__ bool tiny_sort_segment(K *sk, uint32_t *sv, int len) {
+  static_assert(N == 2 || N == 4 || N == 8, "network widths 2, 4, 8");
+  using Ord = KeyOrder<K>;
+  using W = TinyWord<typename Ord::Bits>;
+  W w[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) w[q] = q < len ? W::make(Ord::to_bits(sk[q]), q) : W::pad();
+  if constexpr (N == 2) {
+    W::cx(w[0], w[1]);
+  } else if constexpr (N == 4) {
+    W::cx(w[0], w[1]); W::cx(w[2], w[3]);
+    W::cx(w[0], w[2]); W::cx(w[1], w[3]);
+    W::cx(w[1], w[2]);
+  } else {
+    W::cx(w[0], w[1]); W::cx(w[2], w[3]); W::cx(w[4], w[5]); W::cx(w[6], w[7]);
+    W::cx(w[0], w[2]); W::cx(w[1], w[3]); W::cx(w[4], w[6]); W::cx(w[5], w[7]);
+    W::cx(w[1], w[2]); W::cx(w[5], w[6]);
+    W::cx(w[0], w[4]); W::cx(w[1], w[5]); W::cx(w[2], w[6]); W::cx(w[3], w[7]);
+    W::cx(w[2], w[4]); W::cx(w[3], w[5]);
+    W::cx(w[1], w[2]); W::cx(w[3], w[4]); W::cx(w[5], w[6]);
+  }
+  // Two keys: about half the pairs are in order already, and skip the writes.
+  if (N == 2 && w[0].slot() == 0) return false;
+  uint32_t v[N];
+  if constexpr (PAIRS) {
+#pragma unroll
+    for (int q = 0; q < N; ++q)
+      if (q < len) v[q] = sv[w[q].slot()];
+  }
+  bool moved = N == 2;
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    if (q < len) {
+      sk[q] = Ord::from_bits(w[q].bits());
+      if constexpr (PAIRS) sv[q] = v[q];
+      moved |= w[q].slot() != q;
+    }
+  }
+  return moved;
+}
+
+// Stores staged elements [0, m) (stage[mis + i] is dst[i]; stage and dst - mis
+// are 16-byte aligned, the granules a StagedSpan copied) back to dst: the
+// granules that lie wholly inside [0, m) as 16-byte stores, the ragged ends
+// element by element.
+template <int NT, typename T>
+__device__ __forceinline__ void store_staged(const T *stage, T *dst, int mis, int m) {
+  constexpr int E = 16 / static_cast<int>(sizeof(T));
+  const int tid = threadIdx.x;
+  const int g0 = (mis + E - 1) / E, g1 = (mis + m) / E;  // whole granules [g0, g1)
+  if (g1 > g0) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(stage);
+    uint4 *out = reinterpret_cast<uint4 *>(dst - mis);
+    for (int g = g0 + tid; g < g1; g += NT) out[g] = src[g];
+    const int h = g0 * E - mis;  // head elements [0, h)
+    const int t = g1 * E - mis;  // tail elements [t, m)
+    if (tid < h) dst[tid] = stage[mis + tid];
+    if (tid < m - t) dst[t + tid] = stage[mis + t + tid];
+  } else {
+    for (int i = tid; i < m; i += NT) dst[i] = stage[mis + i];
+  }
+}
 
 // Shared memory: two staging buffers (keys, values, segment starts of a
-// chunk: the granules that cover them), then the segment of every position
-// of the chunk being ranked, as its start | length << 12 in 16 bits.  For
-// 32-bit pairs (CAP 4096) that is 104 KB, and two CTAs fit an SM.
+// chunk: the granules that cover them).  For 32-bit pairs (CAP 4096) that
+// is 96 KB, and two CTAs fit an SM.
 template <typename K, bool PAIRS, int CAP>
 struct TinyLayout {
-  static_assert(CAP <= 4096, "segment starts are packed in 12 bits");
   static constexpr size_t up16(size_t x) { return (x + 15) / 16 * 16; }
   static constexpr int kOffsCap = CAP;  // segment starts staged per chunk
   static constexpr size_t kStageKeys = up16((CAP + 32 / sizeof(K)) * sizeof(K));
   static constexpr size_t kStageVals = PAIRS ? up16((CAP + 8) * sizeof(uint32_t)) : 0;
   static constexpr size_t kStageOffs = up16((kOffsCap + 8) * sizeof(int32_t));
   static constexpr size_t kStage = kStageKeys + kStageVals + kStageOffs;
-  static constexpr size_t kBounds = 2 * kStage;  // uint16[CAP]
-  static constexpr size_t kBytes = kBounds + CAP * sizeof(uint16_t);
+  static constexpr size_t kBytes = 2 * kStage;
 };
 
 template <typename K, bool PAIRS, int NT, int CAP, int MINB>
@@ -49,8 +155,6 @@ tile_tiny_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                  int64_t radix_min, TileChunk *fallback, uint32_t *fallback_count,
                  int64_t max_fallback) {
   using TL = TinyLayout<K, PAIRS, CAP>;
-  using Ord = KeyOrder<K>;
-  using Bits = typename Ord::Bits;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ TilePlan plans[kPlanRing];
   __shared__ __align__(8) uint64_t bars[2];
@@ -58,7 +162,6 @@ tile_tiny_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
   const int64_t t0 = blockIdx.x, G = gridDim.x;
   if (t0 >= ntiles) return;
   const int64_t iters = (ntiles - t0 + G - 1) / G;  // tiles of this CTA: t0 + i * G
-  uint16_t *bd = reinterpret_cast<uint16_t *>(smem + TL::kBounds);
   auto stage_k = [&](int s) { return reinterpret_cast<K *>(smem + s * TL::kStage); };
   auto stage_v = [&](int s) {
     return reinterpret_cast<uint32_t *>(smem + s * TL::kStage + TL::kStageKeys);
@@ -138,64 +241,43 @@ tile_tiny_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
       const TileChunk C = P.c[0];
       const int m = C.m, cnt = C.hi - C.lo;
       const int64_t a = C.a;
-      // Tiny: one segment of at most kTinyMax keys, or staged starts whose
-      // segments are all that short (uniform over the CTA).  A CAP-run of a
-      // long segment (cnt == 0) never is.
-      bool tiny = false;
-      int mis_o = 0;
-      if (cnt == 1) {
-        tiny = m <= kTinyMax;
-      } else if (cnt > 1 && cnt <= TL::kOffsCap) {
-        mis_o = StagedSpan<int32_t>(off.p + C.lo, cnt).mis;
-        const int32_t *so = stage_o(s) + mis_o;
-        bool too_long = false;
-        for (int j = tid; j < cnt; j += NT) {
-          const int64_t b0 = clamp_offset(so[j], off.n);
-          const int64_t e0 = j + 1 < cnt ? clamp_offset(so[j + 1], off.n) : a + m;
-          too_long |= e0 - b0 > kTinyMax;
-        }
-        tiny = !__syncthreads_or(too_long);
-      }
-      if (tiny) {
-        // Bounds of every position, then every key to its place.
-        auto local = [&](int64_t v) {
-          const int64_t x = v - a;
+      // Tiny: one segment, or staged starts.  Every thread sorts whole
+      // segments in the staging buffer; a segment longer than kTinyMax keys
+      // sends the chunk to the list (its keys in global memory are still
+      // untouched), otherwise the chunk goes back to global memory, unless
+      // no key moved.  A CAP-run of a long segment (cnt == 0) is listed.
+      const bool staged_offs = cnt > 1 && cnt <= TL::kOffsCap;
+      if (cnt == 1 || staged_offs) {
+        const int mis_k = StagedSpan<K>(keys + a, m).mis;
+        const int mis_v = PAIRS ? StagedSpan<uint32_t>(vals + a, m).mis : 0;
+        K *sk = stage_k(s) + mis_k;
+        uint32_t *sv = PAIRS ? stage_v(s) + mis_v : nullptr;
+        const int32_t *so =
+            stage_o(s) + (staged_offs ? StagedSpan<int32_t>(off.p + C.lo, cnt).mis : 0);
+        auto local = [&](int32_t v) {
+          const int64_t x = clamp_offset(v, off.n) - a;
           return static_cast<int>(x < 0 ? 0 : (x > m ? m : x));
         };
-        if (cnt == 1) {
-          for (int x = tid; x < m; x += NT) bd[x] = static_cast<uint16_t>(m << 12);
-        } else {
-          const int32_t *so = stage_o(s) + mis_o;
-          for (int j = tid; j < cnt; j += NT) {
-            const int b0 = local(clamp_offset(so[j], off.n));
-            const int e0 = j + 1 < cnt ? local(clamp_offset(so[j + 1], off.n)) : m;
-            const int len = min(e0 - b0, kTinyMax);
-            const uint16_t packed = static_cast<uint16_t>(b0 | (len << 12));
-            for (int x = b0; x < b0 + len; ++x) bd[x] = packed;
+        bool too_long = false, moved = false;
+        for (int j = tid; j < cnt; j += NT) {
+          const int b0 = cnt > 1 ? local(so[j]) : 0;
+          const int e0 = j + 1 < cnt ? local(so[j + 1]) : m;
+          const int len = e0 - b0;
+          if (len > kTinyMax) {
+            too_long = true;
+          } else if (len > 4) {
+            moved |= tiny_sort_segment<8, K, PAIRS>(sk + b0, PAIRS ? sv + b0 : nullptr, len);
+          } else if (len > 2) {
+            moved |= tiny_sort_segment<4, K, PAIRS>(sk + b0, PAIRS ? sv + b0 : nullptr, len);
+          } else if (len == 2) {
+            moved |= tiny_sort_segment<2, K, PAIRS>(sk + b0, PAIRS ? sv + b0 : nullptr, 2);
           }
         }
-        __syncthreads();
-        const K *sk = stage_k(s) + StagedSpan<K>(keys + a, m).mis;
-        const uint32_t *sv =
-            PAIRS ? stage_v(s) + StagedSpan<uint32_t>(vals + a, m).mis : nullptr;
-        for (int e = tid; e < m; e += NT) {
-          const uint32_t u = bd[e];
-          const int b0 = min(static_cast<int>(u & 0xFFFu), m);
-          const int e0 = min(b0 + static_cast<int>(u >> 12), m);
-          const K key = sk[e];
-          const Bits kb = Ord::to_bits(key);
-          int r = 0;
-          for (int x = b0; x < e0; ++x) {
-            const Bits b = Ord::to_bits(sk[x]);
-            r += (b < kb) | ((b == kb) & (x < e));
-          }
-          const int p = b0 + r;
-          // A warp whose keys all stay where they are writes nothing (every
-          // segment of length 1, or already in order).
-          if (__any_sync(__activemask(), p != e) && p < m) {  // p < m: always, with
-            keys[a + p] = key;                                // well-formed offsets
-            if constexpr (PAIRS) vals[a + p] = sv[e];
-          }
+        if (__syncthreads_or(too_long)) {
+          if (tid == 0) list(C);
+        } else if (__syncthreads_or(moved)) {
+          store_staged<NT>(stage_k(s), keys + a, mis_k, m);
+          if constexpr (PAIRS) store_staged<NT>(stage_v(s), vals + a, mis_v, m);
         }
       } else if (tid == 0) {
         list(C);

@@ -2,7 +2,7 @@
 against the oracle.
 
 Problems whose segments average at most SEGSORT_PARAM_TINY_MAX_AVG keys take
-a persistent kernel that keeps two tiles' copies in flight and rank-sorts
+a persistent kernel that keeps two tiles' copies in flight and network-sorts
 every chunk whose segments are at most 8 keys; other chunks (longer
 segments, CAP-runs of long ones, a tile's later chunks) go to the fallback
 list for the comparison sort.  Every case runs with the route forced on for
@@ -40,7 +40,7 @@ def test_equal_segments(pkg, cuda, oracle, inst, route, length, bits):
 def test_random_short_and_some_long(pkg, cuda, oracle, inst, route):
     rng = np.random.default_rng(121)
     lens = rng.integers(0, 9, 60000)
-    lens[::5000] = rng.integers(9, 300, len(lens[::5000]))  # chunks the rank sort lists
+    lens[::5000] = rng.integers(9, 300, len(lens[::5000]))  # chunks the tiny kernel lists
     lens[7777] = 50000                                       # a long segment: CAP-runs and merges
     lens[33333] = 9000
     off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
@@ -74,3 +74,18 @@ def test_key_types(pkg, cuda, oracle, inst, route, dtype):
         keys = inst.uniform_keys(n, seed=129, bits=64, dtype=np.uint64)
         keys[::3] &= np.uint64(0xFF)
     check_both(pkg, cuda, oracle, keys, off)
+
+
+def test_presorted_and_mixed(pkg, cuda, oracle, inst, route):
+    """Chunks whose keys are already in order go back unwritten; the others
+    around them are still sorted (the decision is per chunk)."""
+    rng = np.random.default_rng(130)
+    lens = rng.integers(1, 9, 40000)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    n = int(off[-1])
+    check_both(pkg, cuda, oracle, np.arange(n, dtype=np.uint32), off)
+    keys = np.arange(n, dtype=np.uint32)
+    keys[n // 3: 2 * n // 3] = inst.uniform_keys(2 * n // 3 - n // 3, seed=131)
+    check_both(pkg, cuda, oracle, keys, off)
+    eq = np.full(n, 7, dtype=np.uint32)  # equal keys: the stable order is the input order
+    check_both(pkg, cuda, oracle, eq, off)
