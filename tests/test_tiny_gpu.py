@@ -29,7 +29,7 @@ def route(request, pkg, cuda):
         yield request.param
 
 
-@pytest.mark.parametrize("length", [1, 2, 3, 4, 5, 7, 8, 9, 12, 40])
+@pytest.mark.parametrize("length", [1, 2, 3, 4, 5, 7, 8, 9, 12, 16, 17, 31, 33, 40, 63, 64, 65])
 @pytest.mark.parametrize("bits", [32, 2])
 def test_equal_segments(pkg, cuda, oracle, inst, route, length, bits):
     n = 100003 // length * length + length // 2  # ragged last segment
@@ -89,3 +89,16 @@ def test_presorted_and_mixed(pkg, cuda, oracle, inst, route):
     check_both(pkg, cuda, oracle, keys, off)
     eq = np.full(n, 7, dtype=np.uint32)  # equal keys: the stable order is the input order
     check_both(pkg, cuda, oracle, eq, off)
+
+
+@pytest.mark.parametrize("top", [8, 16, 64])
+def test_random_lengths_up_to(pkg, cuda, oracle, inst, route, top):
+    """Lengths spread over [0, top]: with top 8 every chunk is sorted by the
+    networks, above it most chunks go to the list (empty segments, single
+    keys and every length below top included)."""
+    rng = np.random.default_rng(140 + top)
+    lens = rng.integers(0, top + 1, 200000 // top)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    n = int(off[-1])
+    check_both(pkg, cuda, oracle, inst.uniform_keys(n, seed=141 + top), off)
+    check_both(pkg, cuda, oracle, inst.uniform_keys(n, seed=142 + top, bits=3), off)
