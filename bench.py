@@ -655,9 +655,9 @@ def run_ours(args) -> None:
     # sub-buckets longer than a tile.  The library runs the tiny route
     # (tile_tiny_kernel, and tile_list_kernel for the chunks it lists) when
     # the average segment is at most tiny_max_avg long, the streamed tile
-    # kernel when it is at most stream_max_avg long, the bucket route (tile_bucket_kernel, and tile_list_kernel for the chunks it
-    # refuses) from bucket_min_avg on, the one-CTA-per-tile comparison sort
-    # between.
+    # kernel when it is at most stream_max_avg long, the bucket route
+    # (tile_bucket_kernel, and tile_list_kernel for the chunks it refuses)
+    # from bucket_min_avg on, the one-CTA-per-tile comparison sort between.
     tile_bytes, stream_bytes, bucket_bytes, long_bytes, idle_tile = {}, {}, {}, {}, []
     tiny_bytes = {}
     for lg in lengths:
