@@ -520,6 +520,8 @@ tile_bucket_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
                    const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
                    uint32_t *__restrict__ tmp_vals, int64_t radix_min, TileChunk *fallback,
                    uint32_t *fallback_count, int64_t max_fallback) {
+  pdl_wait();     // the classify kernel's map and jobs
+  pdl_trigger();  // the list kernel may launch under this one (it waits for it)
   bucket_tile<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x, tmp_keys, tmp_vals,
                                  radix_min, fallback, fallback_count, max_fallback, 0);
 }
@@ -535,6 +537,7 @@ tile_list_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
   __shared__ uint32_t hb[Cfg::CAP / 32];
   __shared__ int warp_s[NT / 16];
   __shared__ int64_t next_s;
+  pdl_wait();  // the list of the kernel before
   const int64_t c = min(static_cast<int64_t>(*count), max_list);
   // Chunks are taken from a ticket counter: a static split over the
   // resident CTAs ends unevenly (chunks cost alike).

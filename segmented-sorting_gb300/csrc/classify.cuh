@@ -144,6 +144,7 @@ __device__ __forceinline__ void add_long_job(const LargeWs<K> &ws, const Offsets
 template <typename K>
 __global__ void __launch_bounds__(256)
 large_classify_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
+  pdl_trigger();  // the tile kernel may launch under this one (it waits for it)
   const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   classify_boundary<K>(off, s, true, cap, half, ws.half_first, ws.halves, ws, 0);
 }
@@ -192,6 +193,7 @@ constexpr int kClassifyWarps = 8;
 template <typename K>
 __global__ void __launch_bounds__((kClassifyWarps + 1) * 32)
 large_classify_halves_kernel(Offsets off, int64_t cap, int64_t half, LargeWs<K> ws) {
+  pdl_trigger();  // the tile kernel may launch under this one (it waits for it)
   __shared__ int64_t lb_s[kClassifyWarps + 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t h = static_cast<int64_t>(blockIdx.x) * kClassifyWarps + w;

@@ -242,15 +242,16 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       const int to = occupancy(tiny_kernel, kTinyThreads, TL::kBytes, tiny_occ, dev);
       const unsigned tgrid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(to) * S->sms, tiles));
-      tiny_kernel<<<tgrid, kTinyThreads, TL::kBytes, stream>>>(
-          keys, vals, O, W.half_first, tiles, true, W.radix_min, W.fallback,
-          W.ctr + kCtrFallback, W.max_fallback);
+      launch_after(tiny_kernel, tgrid, kTinyThreads, TL::kBytes, stream, keys, vals, O,
+                   static_cast<const int32_t *>(W.half_first), tiles, true, W.radix_min,
+                   W.fallback, W.ctr + kCtrFallback, W.max_fallback);
       const int lo = occupancy(list_kernel, Cfg::NT, Cfg::kSmemBytes, tlist_occ, dev);
       const unsigned lgrid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, tiles));
-      list_kernel<<<lgrid, Cfg::NT, Cfg::kSmemBytes, stream>>>(
-          keys, vals, O, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
-          W.max_fallback, W.ctr + kCtrListTicket);
+      launch_after(list_kernel, lgrid, Cfg::NT, Cfg::kSmemBytes, stream, keys, vals, O,
+                   W.tmp_keys, W.tmp_vals, static_cast<const TileChunk *>(W.fallback),
+                   static_cast<const uint32_t *>(W.ctr + kCtrFallback), W.max_fallback,
+                   W.ctr + kCtrListTicket);
       rec.tile_launches = 2;
     } else if (short_avg) {
       using SL = StreamLayout<Cfg, K, PAIRS>;
@@ -265,9 +266,9 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       const int so = occupancy(stream_kernel, Cfg::NT, SL::kBytes, stream_occ, dev);
       const unsigned grid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(so) * S->sms, tiles));
-      stream_kernel<<<grid, Cfg::NT, SL::kBytes, stream>>>(keys, vals, O, W.half_first,
-                                                           W.tmp_keys, W.tmp_vals, tiles,
-                                                           W.radix_min);
+      launch_after(stream_kernel, grid, Cfg::NT, SL::kBytes, stream, keys, vals, O,
+                   static_cast<const int32_t *>(W.half_first), W.tmp_keys, W.tmp_vals, tiles,
+                   W.radix_min);
     } else if (bucket_min > 0 && (msd || n >= bucket_min * static_cast<int64_t>(nseg))) {
       // Bucket route: the bucket kernel sorts the chunks it can and lists the
       // others; persistent comparison-sort CTAs take the list.
@@ -284,19 +285,21 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
         rc = SEGSORT_ERR_CUDA;
         break;
       }
-      bucket_kernel<<<static_cast<unsigned>(tiles), BCfg::NT, kBSmem, stream>>>(
-          keys, vals, O, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min, W.fallback,
-          W.ctr + kCtrFallback, W.max_fallback);
+      launch_after(bucket_kernel, static_cast<unsigned>(tiles), BCfg::NT, kBSmem, stream, keys,
+                   vals, O, static_cast<const int32_t *>(W.half_first), W.tmp_keys, W.tmp_vals,
+                   W.radix_min, W.fallback, W.ctr + kCtrFallback, W.max_fallback);
       const int lo = occupancy(list_kernel, Cfg::NT, Cfg::kSmemBytes, list_occ, dev);
       const unsigned lgrid =
           static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(lo) * S->sms, tiles));
-      list_kernel<<<lgrid, Cfg::NT, Cfg::kSmemBytes, stream>>>(
-          keys, vals, O, W.tmp_keys, W.tmp_vals, W.fallback, W.ctr + kCtrFallback,
-          W.max_fallback, W.ctr + kCtrListTicket);
+      launch_after(list_kernel, lgrid, Cfg::NT, Cfg::kSmemBytes, stream, keys, vals, O,
+                   W.tmp_keys, W.tmp_vals, static_cast<const TileChunk *>(W.fallback),
+                   static_cast<const uint32_t *>(W.ctr + kCtrFallback), W.max_fallback,
+                   W.ctr + kCtrListTicket);
       rec.tile_launches = 2;
     } else {
-      tile_kernel<<<static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream>>>(
-          keys, vals, O, W.half_first, W.tmp_keys, W.tmp_vals, W.radix_min);
+      launch_after(tile_kernel, static_cast<unsigned>(tiles), Cfg::NT, Cfg::kSmemBytes, stream,
+                   keys, vals, O, static_cast<const int32_t *>(W.half_first), W.tmp_keys,
+                   W.tmp_vals, W.radix_min);
     }
     if (prof) rec.t1 = prof_event(stream);
     if (cudaGetLastError() != cudaSuccess) {

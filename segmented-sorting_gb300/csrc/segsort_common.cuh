@@ -140,4 +140,16 @@ __device__ __forceinline__ void raise_status(uint32_t bits) {
 
 __host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
 
+// Programmatic dependent launch (PTX griddepcontrol).  A kernel launched with
+// programmatic stream serialization may start while the kernel before it on
+// the stream is still running; pdl_wait() returns once that kernel has
+// completed and its writes are visible (at once for an ordinary launch).
+// pdl_trigger() lets the next such kernel start launching: it is issued at
+// the start of a kernel, and a dependent launches only after every CTA of
+// this grid has issued it or exited, so every CTA is resident by then.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 }  // namespace segsort

@@ -10,6 +10,7 @@
 #include <mutex>
 #include <shared_mutex>
 #include <unordered_map>
+#include <utility>
 
 #include <cuda_runtime.h>
 
@@ -347,6 +348,25 @@ inline cudaMemPool_t device_pool(DeviceState &S, int dev) {
     if (e == cudaSuccess) S.pool_made.store(true, std::memory_order_release);
   });
   return S.pool_err == cudaSuccess ? S.pool : nullptr;
+}
+
+// Launches a kernel that begins with pdl_wait() right behind the kernel
+// before it on the stream (programmatic stream serialization): its CTAs may
+// be scheduled while that kernel finishes.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_after(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                         cudaStream_t stream, Args &&...args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // Opt a kernel into more than 48 KB of dynamic shared memory once per device.

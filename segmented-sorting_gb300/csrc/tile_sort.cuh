@@ -881,6 +881,7 @@ __global__ void __launch_bounds__(NT, MINB)
 tile_sort_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
                  const int32_t *__restrict__ half_first, K *__restrict__ tmp_keys,
                  uint32_t *__restrict__ tmp_vals, int64_t radix_min) {
+  pdl_wait();  // the classify kernel's map and jobs
   tile_cta<K, PAIRS, NT, KPT>(keys, vals, off, half_first, blockIdx.x, tmp_keys, tmp_vals,
                               radix_min);
 }

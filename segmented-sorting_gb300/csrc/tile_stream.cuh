@@ -184,6 +184,7 @@ tile_stream_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets of
 
   const int tid = threadIdx.x;
   const int64_t t0 = blockIdx.x, G = gridDim.x;
+  pdl_wait();  // the classify kernel's map and jobs
   if (t0 >= ntiles) return;
   const int64_t iters = (ntiles - t0 + G - 1) / G;  // tiles of this CTA: t0 + i * G
   const bool runs = tmp_keys != nullptr;

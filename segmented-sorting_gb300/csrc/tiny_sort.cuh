@@ -160,6 +160,8 @@ tile_tiny_kernel(K *__restrict__ keys, uint32_t *__restrict__ vals, Offsets off,
   __shared__ __align__(8) uint64_t bars[2];
   const int tid = threadIdx.x;
   const int64_t t0 = blockIdx.x, G = gridDim.x;
+  pdl_wait();     // the classify kernel's map and jobs
+  pdl_trigger();  // the list kernel may launch under this one (it waits for it)
   if (t0 >= ntiles) return;
   const int64_t iters = (ntiles - t0 + G - 1) / G;  // tiles of this CTA: t0 + i * G
   auto stage_k = [&](int s) { return reinterpret_cast<K *>(smem + s * TL::kStage); };
