@@ -206,6 +206,9 @@ long_segment_kernel(Space sp, LargeWs<K> ws, int64_t cap) {
   __shared__ uint64_t carry_s;
   __shared__ int maxp_s;
 
+  // The MSD route's rank kernel may launch under this one (it waits for it);
+  // every CTA of this cooperative grid is resident before it can.
+  pdl_trigger();
   radix_phases<K, PAIRS, NT>(sp, ws, smem, warp_s);
   if (ws.msd_stage) return;  // the merge passes run after the tile sort of the sub-buckets
 

@@ -58,6 +58,8 @@ inline int64_t msd_stage2_segments(int64_t nseg, int64_t max_rjobs) {
 // and disjoint, so the begins differ) and the MSD jobs before it.
 template <typename K>
 __global__ void __launch_bounds__(256) msd_rank_kernel(LargeWs<K> ws, MsdWs M) {
+  pdl_wait();     // stage 1's jobs and bucket starts
+  pdl_trigger();  // the expansion may launch under this one
   const int32_t nj = min(static_cast<int32_t>(ld_volatile(&ws.ctr[kCtrRJobs])), ws.max_rjobs);
   const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (q == 0 && nj == 0) M.jextra[0] = 0;
@@ -85,6 +87,8 @@ __global__ void __launch_bounds__(256) msd_rank_kernel(LargeWs<K> ws, MsdWs M) {
 // bounded by c_len, so malformed offsets cannot reach outside the arrays.
 template <typename K>
 __global__ void __launch_bounds__(256) msd_expand_kernel(Offsets off, LargeWs<K> ws, MsdWs M) {
+  pdl_wait();     // the jobs' ranks
+  pdl_trigger();  // the sub-bucket kernel may launch under this one
   const int32_t nj = min(static_cast<int32_t>(ld_volatile(&ws.ctr[kCtrRJobs])), ws.max_rjobs);
   const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t all_extra = M.jextra[nj];
@@ -122,6 +126,7 @@ __global__ void __launch_bounds__(256) msd_expand_kernel(Offsets off, LargeWs<K>
 // sub-bucket's keys share (the digits above and at the top varying digit).
 template <typename K>
 __global__ void __launch_bounds__(kRBuckets) msd_sub_kernel(LargeWs<K> ws, MsdWs M) {
+  pdl_wait();  // the expanded offsets
   constexpr int64_t D = sizeof(typename KeyOrder<K>::Bits);
   const int32_t nj = min(static_cast<int32_t>(ld_volatile(&ws.ctr[kCtrRJobs])), ws.max_rjobs);
   const int32_t r = blockIdx.x;

@@ -181,10 +181,13 @@ int sort_impl(K *keys, uint32_t *vals, int64_t n, const int32_t *offsets, int32_
       rc = launch_long(W);
       W.msd_stage = 0;
       if (rc != SEGSORT_OK) break;
-      msd_rank_kernel<K><<<static_cast<unsigned>((W.max_rjobs + 255) / 256), 256, 0, stream>>>(W, M);
-      msd_expand_kernel<K><<<static_cast<unsigned>((std::max<int64_t>(nseg, c_len) + 256) / 256),
-                             256, 0, stream>>>(off, W, M);
-      msd_sub_kernel<K><<<static_cast<unsigned>(W.max_rjobs), kRBuckets, 0, stream>>>(W, M);
+      launch_after(msd_rank_kernel<K>, static_cast<unsigned>((W.max_rjobs + 255) / 256), 256, 0,
+                   stream, W, M);
+      launch_after(msd_expand_kernel<K>,
+                   static_cast<unsigned>((std::max<int64_t>(nseg, c_len) + 256) / 256), 256, 0,
+                   stream, off, W, M);
+      launch_after(msd_sub_kernel<K>, static_cast<unsigned>(W.max_rjobs), kRBuckets, 0, stream, W,
+                   M);
       if (prof) rec.m1 = prof_event(stream);
       if (cudaGetLastError() != cudaSuccess) {
         rc = SEGSORT_ERR_CUDA;
