@@ -56,6 +56,24 @@ METRIC = "segsort Gkeys/s vs segment size, % HBM roofline; batched/served p50/p9
 WORKLOAD = ("equal-segment sweep: 2^24 uint32 key/value pairs per instance, keys uniform "
             "in [0,2^32), values = index, segment length 2^1..2^20 (one instance each)")
 BYTES_PER_PAIR = 16  # read key+value once, write key+value once
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest x over the job's ranks (x itself for one rank): the
+    timed region of a multi-rank run is its slowest rank's."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gkeys(keys_per_step: int, steps: int, world: int, ms: float) -> float:
+    """Whole-job throughput: the keys every rank sorted (each rank sorts its
+    own replica of the workload) over the slowest rank's time."""
+    return keys_per_step * steps * world / (ms * 1e-3) / 1e9
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -570,13 +588,9 @@ def run_ours(args) -> None:
                 evs[lg].append((a, b))
         t_end.record(stream)
         barrier()
-    region_ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        t = torch.tensor([region_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        region_ms = float(t.item())
+    region_ms = max_over_ranks(t_start.elapsed_time(t_end), world, dev)
     keys_per_step = n * len(lengths)
-    value = keys_per_step * args.steps * world / (region_ms * 1e-3) / 1e9
+    value = whole_job_gkeys(keys_per_step, args.steps, world, region_ms)
     if pkg.device_status() != 0:
         raise RuntimeError("device status reports a bounded wait that gave up")
 
@@ -762,12 +776,8 @@ def run_ours(args) -> None:
         join()
         b.record(stream)
         barrier()
-        e_ms = a.elapsed_time(b)
-        if world > 1:
-            t = torch.tensor([e_ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
-        e2e = {"value": keys_per_step * e_steps * world / (e_ms * 1e-3) / 1e9, "unit": "Gkeys/s",
+        e_ms = max_over_ranks(a.elapsed_time(b), world, dev)
+        e2e = {"value": whole_job_gkeys(keys_per_step, e_steps, world, e_ms), "unit": "Gkeys/s",
                "h2d_bytes_per_step": 8 * n * len(lengths),
                "d2h_bytes_per_step": 8 * n * len(lengths),
                "steps": e_steps, "ms_per_step": e_ms / e_steps}
