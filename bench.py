@@ -185,9 +185,20 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 def bench_config(n: int, lengths: list[int], world: int) -> dict:
-    """The workload's config, identical for both arms."""
-    return {"workload": WORKLOAD, "n": n, "log2_lengths": lengths,
-            "l2": "inputs larger than L2: 128 MiB fresh instance per call",
+    """The workload's config, identical for both arms.  The default run is
+    WORKLOAD; other sizes and length lists are named by what they are."""
+    log_n = n.bit_length() - 1
+    if n == 1 << 24 and lengths == list(range(1, 21)):
+        workload = WORKLOAD
+    else:
+        span = (f"2^{lengths[0]}..2^{lengths[-1]}" if lengths == list(range(lengths[0], lengths[-1] + 1))
+                else ", ".join(f"2^{x}" for x in lengths))
+        workload = (f"equal-segment sweep: 2^{log_n} uint32 key/value pairs per instance, keys "
+                    f"uniform in [0,2^32), values = index, segment length {span} (one instance each)")
+    mib = 8 * n / 2**20
+    l2 = (f"inputs larger than L2: {mib:g} MiB fresh instance per call" if 8 * n > 129e6
+          else f"inputs smaller than L2 ({mib:g} MiB fresh instance per call)")
+    return {"workload": workload, "n": n, "log2_lengths": lengths, "l2": l2,
             "parallelism": f"replicas{world}"}
 
 

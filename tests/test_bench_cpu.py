@@ -96,3 +96,13 @@ def test_reference_arm_under_torchrun():
     lines = _json_lines(r.stdout)
     assert len(lines) == 1  # rank 0 alone prints
     _check_reference_line(lines[0], 2)
+
+
+def test_config_names_the_workload():
+    """The default run is the sweep of 2^24-pair instances over lengths 2^1..2^20,
+    above L2; other runs say what they are, and whether they fit in L2."""
+    d = bench.bench_config(1 << 24, list(range(1, 21)), 1)
+    assert d["workload"] == bench.WORKLOAD and d["l2"].startswith("inputs larger than L2: 128 MiB")
+    small = bench.bench_config(1 << 20, [1, 10, 18], 2)
+    assert "2^20 uint32" in small["workload"] and "2^1, 2^10, 2^18" in small["workload"]
+    assert small["l2"].startswith("inputs smaller than L2") and small["parallelism"] == "replicas2"
