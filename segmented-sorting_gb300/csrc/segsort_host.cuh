@@ -352,7 +352,9 @@ inline cudaMemPool_t device_pool(DeviceState &S, int dev) {
 
 // Launches a kernel that begins with pdl_wait() right behind the kernel
 // before it on the stream (programmatic stream serialization): its CTAs may
-// be scheduled while that kernel finishes.
+// be scheduled while that kernel finishes.  A failed launch is also recorded
+// for cudaGetLastError(), which the sort checks after each stage, as for its
+// <<<>>> launches.
 template <typename... KArgs, typename... Args>
 cudaError_t launch_after(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
                          cudaStream_t stream, Args &&...args) {
