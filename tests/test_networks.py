@@ -14,6 +14,11 @@
   csrc/tile_stream.cuh): the bulk copy starts on a 16-byte boundary inside
   the range's first granule, covers every element, and stays inside the
   staging buffer (CAP + 32 / sizeof(T) elements, CAP/2 + 8 for offsets).
+* The tiny route's networks (tiny_sort_segment in csrc/tiny_sort.cuh, read
+  from the source) sort every 0-1 input of 2, 4 and 8 words with 1, 5 and 19
+  comparators, and over (order bits, slot) composites with padded slots give
+  the stable order; store_staged writes every element of a chunk exactly
+  once whatever its misalignment.
 """
 from __future__ import annotations
 
@@ -148,3 +153,83 @@ def test_staged_span_geometry(elem):
                 assert nvec * v <= stage_cap     # inside the staging buffer
                 # the last granule holds the range's last element (no granule past it)
                 assert (copy_from + 16 * nvec) - (byte0 + m * elem) < 16
+
+
+# ---------------------------------------------------------------------------
+# The tiny route (csrc/tiny_sort.cuh): the comparators of tiny_sort_segment
+# are read from the source, so the check covers the networks the kernel runs.
+TINY_SRC = (__import__("pathlib").Path(__file__).resolve().parents[1]
+            / "segmented-sorting_gb300" / "csrc" / "tiny_sort.cuh")
+
+
+def tiny_networks() -> dict[int, list[tuple[int, int]]]:
+    import re
+    src = TINY_SRC.read_text()
+    body = src[src.index("bool tiny_sort_segment("):]
+    body = body[body.index("if constexpr (N == 2) {"):body.index("// Two keys")]
+    n2, rest = body.split("} else if constexpr (N == 4) {")
+    n4, n8 = rest.split("} else {")
+    pat = re.compile(r"W::cx\(w\[(\d+)\], w\[(\d+)\]\)")
+    return {n: [(int(a), int(b)) for a, b in pat.findall(part)]
+            for n, part in ((2, n2), (4, n4), (8, n8))}
+
+
+@pytest.mark.parametrize("n,size", [(2, 1), (4, 5), (8, 19)])
+def test_tiny_networks_sort_every_input(n, size):
+    pairs = tiny_networks()[n]
+    assert len(pairs) == size and all(a < b < n for a, b in pairs)
+    x = zero_one_inputs(n)
+    for a, b in pairs:
+        lo = np.minimum(x[:, a], x[:, b])
+        hi = np.maximum(x[:, a], x[:, b])
+        x[:, a], x[:, b] = lo, hi
+    assert np.all(np.diff(x, axis=1) >= 0)
+
+
+@pytest.mark.parametrize("n", [2, 4, 8])
+def test_tiny_composites_give_the_stable_order(n):
+    """Every segment length up to the network's width: (order bits << 6 | slot)
+    composites, the slots past the segment padded with the largest value, come
+    out as the stable order of the keys (few distinct keys: many ties)."""
+    pairs = tiny_networks()[n]
+    rng = np.random.default_rng(7 + n)
+    pad = (1 << 64) - 1
+    for length in range(1, n + 1):
+        for _ in range(300):
+            keys = [int(k) for k in rng.integers(0, 3, length)]
+            keys[0] = (1 << 32) - 1 if rng.random() < 0.2 else keys[0]  # the largest key too
+            w = [(k << 6) | q for q, k in enumerate(keys)] + [pad] * (n - length)
+            for a, b in pairs:
+                if w[a] > w[b]:
+                    w[a], w[b] = w[b], w[a]
+            got = [(x >> 6, x & 63) for x in w[:length]]
+            want = sorted(((k, q) for q, k in enumerate(keys)), key=lambda t: t[0])  # stable
+            assert got == want and all(x == pad for x in w[length:])
+
+
+@pytest.mark.parametrize("elem", [4, 8])
+def test_store_staged_writes_each_element_once(elem):
+    """store_staged's split of [0, m) into whole 16-byte granules and the
+    ragged head and tail, restated: every element is written exactly once and
+    nothing outside [0, m), for every misalignment, chunk size and block size."""
+    e = 16 // elem
+    for nt in (32, 512):
+        for mis in range(e):
+            for m in list(range(0, 70)) + [2047, 2048, 4095, 4096]:
+                writes = [0] * (m + 2 * e)  # index i + e is element i
+                g0, g1 = (mis + e - 1) // e, (mis + m) // e
+                if g1 > g0:
+                    for g in range(g0, g1):            # granule g covers elements g*e - mis ..
+                        for c in range(e):
+                            writes[g * e - mis + c + e] += 1
+                    h, t = g0 * e - mis, g1 * e - mis
+                    for tid in range(nt):
+                        if tid < h:
+                            writes[tid + e] += 1
+                        if tid < m - t:
+                            writes[t + tid + e] += 1
+                else:
+                    for i in range(m):
+                        writes[i + e] += 1
+                assert writes[e:e + m] == [1] * m, (nt, mis, m)
+                assert sum(writes) == m, (nt, mis, m)
