@@ -23,7 +23,7 @@ Printed JSON line (rank 0):
               CPU algorithm, src/mseq.cu:44-49) on the same full instances:
               one step on all host threads and one on a single thread (the
               reference's mseq is sequential)
-  per_len     per segment length: ms, Gkeys/s and fraction of the HBM roofline
+  per_len     per segment length: ms, Gkeys/s, fraction of the HBM roofline and route
   batched, served, configs   the other workloads (64-instance batch, Poisson
               request stream, 2^20 keys-only, 2^25 lognormal, low entropy)
 
@@ -685,28 +685,38 @@ def run_ours(args) -> None:
     # from bucket_min_avg on, the one-CTA-per-tile comparison sort between.
     tile_bytes, stream_bytes, bucket_bytes, long_bytes, idle_tile = {}, {}, {}, {}, []
     tiny_bytes = {}
+    route = {}  # per length, the route its call takes (reported with per_len)
     for lg in lengths:
         ln = 1 << lg
         full = BYTES_PER_PAIR * n + 4 * (n // ln + 1)
-        tile_table = bucket_bytes if bucket_min_avg and ln >= bucket_min_avg else tile_bytes
+        bucket = bool(bucket_min_avg) and ln >= bucket_min_avg
+        tile_table = bucket_bytes if bucket else tile_bytes
         if ln <= stream_max_avg and ln <= tiny_max_avg:
             tiny_bytes[lg] = full
+            route[lg] = "tiny"
         elif ln <= stream_max_avg:
             stream_bytes[lg] = full
+            route[lg] = "streamed tile"
         elif ln <= cap:
             tile_table[lg] = full
+            route[lg] = "bucket" if bucket else "comparison tile"
         elif ln <= radix_min:
             tile_table[lg] = full
             long_bytes[lg] = BYTES_PER_PAIR * n * merge_passes(ln)
+            route[lg] = f"{'bucket' if bucket else 'comparison'}-sorted runs + {merge_passes(ln)} merge passes"
         else:
             digits = varying_digits(lg)
             if msd_on and len(digits) >= 3:
                 bucket_bytes[lg] = BYTES_PER_PAIR * n
                 long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n + msd_oversize_bytes(lg, digits[-1])
+                route[lg] = "MSD radix pass + bucket sort of the sub-buckets"
             else:
                 idle_tile.append(lg)  # the tile kernel finds no work: every segment is on the radix route
                 passes = len(digits)
                 long_bytes[lg] = 4 * n + BYTES_PER_PAIR * n * (passes + (passes & 1))
+                route[lg] = f"LSD radix, {passes} passes"
+    for p in per_len:
+        p["route"] = route[p["log2_len"]]
     kernels = {}
     for name, table, key in (("tile_sort_kernel", tile_bytes, "tile_ms"),
                              ("tile_tiny_kernel", tiny_bytes, "tile_ms"),
