@@ -18,7 +18,8 @@
   from the source) sort every 0-1 input of 2, 4 and 8 words with 1, 5 and 19
   comparators, and over (order bits, slot) composites with padded slots give
   the stable order; store_staged writes every element of a chunk exactly
-  once whatever its misalignment.
+  once whatever its misalignment; its kernel's schedule of plans, copies
+  and barrier phases (restated) never reads a plan or stage early or late.
 """
 from __future__ import annotations
 
@@ -233,3 +234,47 @@ def test_store_staged_writes_each_element_once(elem):
                         writes[i + e] += 1
                 assert writes[e:e + m] == [1] * m, (nt, mis, m)
                 assert sum(writes) == m, (nt, mis, m)
+
+
+@pytest.mark.parametrize("iters", list(range(1, 40)) + [64, 100])
+def test_tiny_kernel_schedule(iters):
+    """tile_tiny_kernel's schedule, restated: plans made kPlanBatch (16) at a
+    time into a ring of kPlanRing (32) by warp 0, copies of iteration i into
+    stage i & 1 issued two iterations ahead, the wait of iteration i on its
+    stage's barrier with parity (i >> 1) & 1.  Every plan is written before
+    the copy or the sort that reads it and is not overwritten while either
+    still needs it; every wait expects the phase its stage is in; a stage is
+    refilled only after the sort of its previous tile has ended."""
+    batch, ring = 16, 32
+    slot_of = {}                      # ring slot -> iteration whose plan it holds
+    phases = [0, 0]                   # completed phases per stage barrier
+    in_flight = [None, None]          # iteration whose copy is in each stage
+
+    def make_plans(i0):
+        for i in range(i0, min(i0 + batch, iters)):
+            slot_of[i % ring] = i
+
+    def issue(i):
+        assert slot_of.get(i % ring) == i          # its plan is there
+        assert in_flight[i & 1] is None            # the stage is free
+        in_flight[i & 1] = i
+
+    make_plans(0)
+    issue(0)
+    if iters > 1:
+        issue(1)
+    for i in range(iters):
+        s = i & 1
+        assert in_flight[s] == i
+        assert phases[s] % 2 == (i >> 1) & 1       # the parity the wait expects
+        phases[s] += 1                             # the copy completes the phase
+        assert slot_of.get(i % ring) == i          # the sort reads its plan
+        in_flight[s] = None                        # end-of-iteration barrier: stage free
+        if i + 2 < iters:
+            if (i + 2) % batch == 0:
+                # the batch overwrites slots (i+2 .. i+17) % 32: none still needed
+                needed = {j % ring for j in (i + 1,) if j < iters}
+                assert not needed & {j % ring for j in range(i + 2, min(i + 2 + batch, iters))}
+                make_plans(i + 2)
+            issue(i + 2)
+    assert in_flight == [None, None]               # no copy outstanding at the end
